@@ -1,0 +1,196 @@
+"""GB300-native GLINT contact-tracing step.
+
+Python mirror of the reference's GPU seam (tracing/process.cpp:373-376):
+
+    bench = cuda_create_device_bench(config, mbr, first_points)   # geometry.cu:1395
+    for t ...:
+        stats = process_with_gpu(bench, points_t, cur_time=t)      # geometry.cu:1573
+        meetings = bench.meetings()                                # meeting.cpp:147-153
+
+Everything runs in libglint.so (hand-written sm_103a CUDA behind the C ABI in
+include/glint.h).  There is no CPU fallback: constructing a DeviceBench
+raises when the library is missing or no GPU is visible.
+"""
+from __future__ import annotations
+
+import ctypes
+import dataclasses
+import os
+
+import numpy as np
+
+from . import _abi
+from ._abi import GlintConfig, GlintStepStats, MEETING_DTYPE, SCHEMA_DTYPE, GlintError
+
+__all__ = [
+    "Configuration", "DeviceBench", "cuda_create_device_bench", "process_with_gpu", "GlintError",
+    "MEETING_DTYPE", "SCHEMA_DTYPE", "library_path", "load_library",
+]
+
+library_path = _abi.library_path
+load_library = _abi.load_library
+
+
+@dataclasses.dataclass
+class Configuration:
+    """The fields of the reference's `configuration` (util/config.h:15-114)
+    that this path reads, with the reference's defaults."""
+    num_objects: int = 1000
+    grid_capacity: int = 50
+    grid_amplify: float = 2.0
+    num_meeting_buckets: int = 0        # 0 -> 2 * num_objects (config.h:176-178)
+    reach_distance: float = 2.0
+    min_meet_time: int = 5
+    max_meet_time: int = 4096
+    schema_update_delay: int = 1
+    dynamic_schema: bool = True
+    phased_lookup: bool = True
+    start_time: int = 0
+    x_buffer: float = 0.0
+    y_buffer: float = 0.0
+    G_bytes: int = 2
+    CTF_count: int = 100
+    dProbFalse: float = 100.0
+    # this implementation
+    precision_mode: int = 0             # 0 plain FP64, 1 FP32 guard band
+    device: int = 0
+    new_capacity: int = 0
+    check_capacity: int = 0
+    meeting_log_capacity: int = 0
+    timing: bool = False
+    auto_flush: bool = False
+
+    def to_c(self) -> GlintConfig:
+        c = GlintConfig()
+        _abi.lib().glint_config_defaults(ctypes.byref(c), int(self.num_objects))
+        for f in dataclasses.fields(self):
+            v = getattr(self, f.name)
+            if isinstance(v, bool):
+                v = int(v)
+            setattr(c, f.name, v)
+        if not self.num_meeting_buckets:
+            c.num_meeting_buckets = 2 * int(self.num_objects)
+        return c
+
+
+class DeviceBench:
+    """Device-resident workbench: schema, leaf tiles, meeting table, meeting log."""
+
+    def __init__(self, config: Configuration, mbr, first_points=None, schema=None):
+        self.lib = _abi.lib()
+        self.config = config
+        self.n = int(config.num_objects)
+        self._cfg = config.to_c()
+        box = _abi.GlintBox()
+        m = np.asarray(mbr, dtype=np.float64).reshape(4)
+        box.low[0], box.low[1], box.high[0], box.high[1] = m
+        self._box = box
+        pts_ptr = None
+        if first_points is not None:
+            self._first = np.ascontiguousarray(first_points, dtype=np.float64).reshape(self.n, 2)
+            pts_ptr = self._first.ctypes.data_as(ctypes.c_void_p)
+        init_ptr = None
+        if schema is not None:
+            init_ptr = ctypes.byref(schema)
+        h = ctypes.c_void_p()
+        st = self.lib.glint_create(ctypes.byref(self._cfg), ctypes.byref(box), pts_ptr, init_ptr, ctypes.byref(h))
+        if st != 0:
+            raise GlintError(st, "glint_create")
+        self.h = h
+        sc = ctypes.c_uint32()
+        gc = ctypes.c_uint32()
+        bk = ctypes.c_uint64()
+        self.lib.glint_get_capacities(self.h, ctypes.byref(sc), ctypes.byref(gc), ctypes.byref(bk))
+        self.schema_capacity, self.grids_capacity, self.num_buckets = sc.value, gc.value, bk.value
+        self._staging = None
+
+    # -- per step -----------------------------------------------------------
+    def step(self, points, cur_time: int) -> GlintStepStats:
+        """process_with_gpu: host points in, synchronous."""
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        if pts.size != 2 * self.n:
+            raise ValueError("points must hold num_objects (lon, lat) pairs")
+        stats = GlintStepStats()
+        st = self.lib.glint_step(self.h, pts.ctypes.data_as(ctypes.c_void_p), int(cur_time), ctypes.byref(stats))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        return stats
+
+    def step_device(self, d_points_ptr: int, cur_time: int):
+        st = self.lib.glint_step_device(self.h, ctypes.c_void_p(int(d_points_ptr)), int(cur_time))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+
+    def sync(self) -> GlintStepStats:
+        stats = GlintStepStats()
+        st = self.lib.glint_sync(self.h, ctypes.byref(stats))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        return stats
+
+    def meetings(self) -> np.ndarray:
+        """Meetings identified by the last step, in bucket order."""
+        n = ctypes.c_uint64()
+        st = self.lib.glint_meetings(self.h, None, 0, ctypes.byref(n))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        out = np.zeros(n.value, dtype=MEETING_DTYPE)
+        if n.value:
+            st = self.lib.glint_meetings(self.h, out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n))
+            if st != 0:
+                raise GlintError(st, self.last_error())
+        return out
+
+    # -- state ------------------------------------------------------------------
+    def schema(self):
+        nodes = np.zeros(self.schema_capacity, dtype=SCHEMA_DTYPE)
+        ss = np.zeros(self.schema_capacity, dtype=np.uint32)
+        gs = np.zeros(self.grids_capacity, dtype=np.uint32)
+        gc = np.zeros(self.grids_capacity, dtype=np.uint32)
+        ssi = ctypes.c_uint32()
+        gsi = ctypes.c_uint32()
+        st = self.lib.glint_get_schema(self.h, nodes.ctypes.data_as(ctypes.c_void_p), ss.ctypes.data_as(ctypes.c_void_p),
+                                       gs.ctypes.data_as(ctypes.c_void_p), gc.ctypes.data_as(ctypes.c_void_p),
+                                       ctypes.byref(ssi), ctypes.byref(gsi))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        return nodes, ss, gs, gc, ssi.value, gsi.value
+
+    def buckets(self):
+        B = int(self.num_buckets)
+        k = np.zeros(B, np.uint64)
+        s = np.zeros(B, np.uint32)
+        m = np.zeros((B, 4), np.float32)
+        st = self.lib.glint_get_buckets(self.h, k.ctypes.data_as(ctypes.c_void_p), s.ctypes.data_as(ctypes.c_void_p),
+                                        m.ctypes.data_as(ctypes.c_void_p))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        return k, s, m
+
+    @property
+    def stream(self) -> int:
+        return int(self.lib.glint_stream(self.h) or 0)
+
+    def last_error(self) -> str:
+        return self.lib.glint_last_error(self.h).decode()
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.glint_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def cuda_create_device_bench(config: Configuration, mbr, first_points=None, schema=None) -> DeviceBench:
+    """Mirror of cuda_create_device_bench (cuda/geometry.cu:1395-1565)."""
+    return DeviceBench(config, mbr, first_points, schema)
+
+
+def process_with_gpu(bench: DeviceBench, points, cur_time: int) -> GlintStepStats:
+    """Mirror of process_with_gpu (cuda/geometry.cu:1573-2218) for one timestep."""
+    return bench.step(points, cur_time)

@@ -1,0 +1,150 @@
+"""ctypes declarations of the C ABI in include/glint.h."""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+library_path = os.path.join(HERE, "libglint.so")
+
+_LIB = None
+
+STATUS = {
+    0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of device memory",
+    4: "device buffer capacity exceeded", 5: "unsupported configuration", 6: "invalid context state",
+    7: "no CUDA device",
+}
+
+
+class GlintError(RuntimeError):
+    def __init__(self, status: int, detail: str = ""):
+        self.status = int(status)
+        super().__init__(f"glint status {status} ({STATUS.get(int(status), '?')}): {detail}")
+
+
+class GlintConfig(ctypes.Structure):
+    _fields_ = [
+        ("num_objects", ctypes.c_uint32),
+        ("grid_capacity", ctypes.c_uint32),
+        ("grid_amplify", ctypes.c_double),
+        ("num_meeting_buckets", ctypes.c_uint64),
+        ("reach_distance", ctypes.c_double),
+        ("min_meet_time", ctypes.c_uint32),
+        ("max_meet_time", ctypes.c_uint32),
+        ("schema_update_delay", ctypes.c_uint32),
+        ("dynamic_schema", ctypes.c_uint32),
+        ("phased_lookup", ctypes.c_uint32),
+        ("start_time", ctypes.c_uint32),
+        ("x_buffer", ctypes.c_double),
+        ("y_buffer", ctypes.c_double),
+        ("G_bytes", ctypes.c_uint32),
+        ("CTF_count", ctypes.c_uint32),
+        ("dProbFalse", ctypes.c_double),
+        ("precision_mode", ctypes.c_uint32),
+        ("device", ctypes.c_uint32),
+        ("new_capacity", ctypes.c_uint64),
+        ("check_capacity", ctypes.c_uint64),
+        ("meeting_log_capacity", ctypes.c_uint64),
+        ("timing", ctypes.c_uint32),
+        ("auto_flush", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32 * 6),
+    ]
+
+
+class GlintBox(ctypes.Structure):
+    _fields_ = [("low", ctypes.c_double * 2), ("high", ctypes.c_double * 2)]
+
+
+class GlintSchemaInit(ctypes.Structure):
+    _fields_ = [
+        ("nodes", ctypes.c_void_p),
+        ("num_nodes", ctypes.c_uint32),
+        ("schema_stack_index", ctypes.c_uint32),
+        ("grids_stack_index", ctypes.c_uint32),
+        ("reserved", ctypes.c_uint32),
+        ("schema_stack", ctypes.c_void_p),
+        ("grids_stack", ctypes.c_void_p),
+    ]
+
+
+class GlintStepStats(ctypes.Structure):
+    _fields_ = [
+        ("cur_time", ctypes.c_uint32),
+        ("checks", ctypes.c_uint32),
+        ("border_objects", ctypes.c_uint32),
+        ("cross_checks", ctypes.c_uint32),
+        ("candidates", ctypes.c_uint64),
+        ("contacts", ctypes.c_uint64),
+        ("new_keys", ctypes.c_uint64),
+        ("num_taken_buckets", ctypes.c_uint64),
+        ("num_active_meetings", ctypes.c_uint32),
+        ("meetings", ctypes.c_uint32),
+        ("splits", ctypes.c_uint32),
+        ("merges", ctypes.c_uint32),
+        ("leaves", ctypes.c_uint32),
+        ("nodes", ctypes.c_uint32),
+        ("dropped_objects", ctypes.c_uint32),
+        ("rechecks", ctypes.c_uint32),
+        ("ambiguous", ctypes.c_uint32),
+        ("band_pairs", ctypes.c_uint32),
+        ("error_flags", ctypes.c_uint32),
+        ("pad", ctypes.c_uint32),
+        ("meeting_log_size", ctypes.c_uint64),
+        ("ms", ctypes.c_float * 8),
+    ]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("pad", "ms")}
+        d["ms"] = list(self.ms)
+        return d
+
+
+MEETING_DTYPE = np.dtype([("pid1", "<u4"), ("pid2", "<u4"), ("start", "<u4"), ("end", "<u4"), ("mbr", "<f4", (4,))])
+SCHEMA_DTYPE = np.dtype([
+    ("grid_id", "<u4"), ("level", "<i2"), ("type", "<i2"), ("overflow_count", "<i2"),
+    ("underflow_count", "<i2"), ("pad", "<u4"), ("mid_x", "<f8"), ("mid_y", "<f8"),
+    ("low", "<f8", (2,)), ("high", "<f8", (2,)), ("children", "<u4", (4,)),
+])
+assert SCHEMA_DTYPE.itemsize == 80 and MEETING_DTYPE.itemsize == 32
+
+
+def load_library(path: str | None = None):
+    """Loads libglint.so; builds it in-tree first when it is missing."""
+    p = path or library_path
+    if not os.path.exists(p):
+        from . import build as _build
+        _build.build()
+    lib = ctypes.CDLL(p)
+    vp = ctypes.c_void_p
+    u32, u64 = ctypes.c_uint32, ctypes.c_uint64
+    lib.glint_abi_version.restype = ctypes.c_int
+    lib.glint_struct_sizes.argtypes = [ctypes.POINTER(ctypes.c_uint32)]
+    lib.glint_status_string.restype = ctypes.c_char_p
+    lib.glint_status_string.argtypes = [ctypes.c_int]
+    lib.glint_config_defaults.argtypes = [ctypes.POINTER(GlintConfig), u32]
+    lib.glint_create.argtypes = [ctypes.POINTER(GlintConfig), ctypes.POINTER(GlintBox), vp, vp, ctypes.POINTER(vp)]
+    lib.glint_destroy.argtypes = [vp]
+    lib.glint_last_error.restype = ctypes.c_char_p
+    lib.glint_last_error.argtypes = [vp]
+    lib.glint_step.argtypes = [vp, vp, u32, ctypes.POINTER(GlintStepStats)]
+    lib.glint_step_device.argtypes = [vp, vp, u32]
+    lib.glint_sync.argtypes = [vp, ctypes.POINTER(GlintStepStats)]
+    lib.glint_meetings.argtypes = [vp, vp, u64, ctypes.POINTER(u64)]
+    lib.glint_get_schema.argtypes = [vp, vp, vp, vp, vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    lib.glint_get_buckets.argtypes = [vp, vp, vp, vp]
+    lib.glint_get_capacities.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u64)]
+    lib.glint_stream.restype = vp
+    lib.glint_stream.argtypes = [vp]
+    lib.glint_gen_create.argtypes = [vp, u32, vp, u32, u32, u32, ctypes.POINTER(vp)]
+    lib.glint_gen_step.argtypes = [vp, vp, vp]
+    lib.glint_gen_destroy.argtypes = [vp]
+    return lib
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        _LIB = load_library()
+    return _LIB

@@ -1,0 +1,188 @@
+/*
+ * glint_internal.cuh -- the device-resident state of one context and the
+ * host launchers of each per-step stage.
+ *
+ * HBM layout (N objects, G grid slots, S schema slots, B buckets):
+ *   points      double2[N]   lon/lat as given, AoS 16 B per object
+ *   L           double[N]    degree_per_meter_longitude(lat) with CUDA sin
+ *   obj_*       u32[N]       leaf grid id, last_valid node, leaf node per object
+ *   sorted      u32[N]       object ids sorted by (grid id, object id): leaf member lists
+ *   sxy, sL     [N]          coordinates and L gathered in that order (leaf tiles)
+ *   nodes       DNode[S]     64-byte schema records, low corners in low[S]
+ *   stacks      u32[S], u32[G]  free schema / grid slots (workbench.h:118-128)
+ *   qlist/tlist              cross-leaf checks, by querier and by target leaf
+ *   tab, stamp  TRec[B], u8[B]  the meeting table (32 B per bucket) and touch stamps
+ *   newlist     (key, prio)  contacts whose pair was absent at the start of the step
+ *   log         glint_meeting ring of identified meetings
+ */
+#ifndef GLINT_INTERNAL_CUH_
+#define GLINT_INTERNAL_CUH_
+
+#include <cuda_runtime.h>
+#include <string>
+
+#include "glint_device.cuh"
+
+namespace glint {
+
+/* counters shared by the kernels of one step; copied to pinned host memory
+ * at the end of each step */
+struct DevCounters {
+    unsigned int cross_checks;
+    unsigned int border_objects;
+    unsigned long long candidates;
+    unsigned long long contacts;
+    unsigned long long new_keys;          /* entries appended to the new list */
+    unsigned long long taken;
+    unsigned int active;
+    unsigned int meetings;
+    unsigned int splits;
+    unsigned int merges;
+    unsigned int dropped;
+    unsigned int rechecks;
+    unsigned int ambiguous;
+    unsigned int band_pairs;
+    unsigned int error_flags;
+    unsigned int n_leaf_work;              /* leaves with at least one object */
+    unsigned int work_next;                /* dynamic scheduling cursor */
+    unsigned int n_events;                 /* schema events this step */
+    unsigned int n_cand;                   /* merge candidates this step */
+    unsigned int total_checks;
+    unsigned int n_big;                    /* leaf segments sorted by a whole block */
+    unsigned int pad[3];
+    /* persistent (not cleared per step) */
+    unsigned int ssi;                      /* schema_stack_index */
+    unsigned int gsi;                      /* grids_stack_index */
+    unsigned long long log_head;           /* meetings written to the log so far */
+    unsigned long long log_step_begin;     /* log position of this step's first meeting */
+};
+/* bytes cleared at the start of every step */
+constexpr size_t kStepCounterBytes = offsetof(DevCounters, ssi);
+
+struct NewEntry {
+    unsigned long long key;
+    unsigned long long prio;
+};
+
+struct SchemaEvent {
+    uint32_t node;
+    uint32_t kind;        /* 0 split, 1 merge */
+};
+
+struct StepTimers {
+    cudaEvent_t ev[9];
+    bool created = false;
+};
+
+} // namespace glint
+
+struct glint_ctx {
+    glint_config cfg;
+    glint_box mbr;
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string last_error;
+
+    uint32_t N = 0, G = 0, S = 0, cap = 0;
+    uint64_t B = 0, Bm = 0;
+    uint64_t check_cap = 0, new_cap = 0, log_cap = 0;
+    uint32_t max_leaf_count = 0;           /* sorter limit for one leaf segment */
+    double x_buffer = 0, y_buffer = 0, dpm_lat = 0, band = 0;
+    uint64_t step_index = 0;
+    uint32_t last_time = 0;
+
+    /* objects */
+    double2 *d_pts = nullptr;
+    double *d_L = nullptr;
+    uint32_t *d_obj_gid = nullptr, *d_obj_lv = nullptr, *d_obj_leaf = nullptr;
+    uint32_t *d_order = nullptr;           /* processing order of the descent */
+    uint32_t *d_grid_count = nullptr;      /* [G+1] */
+    uint32_t *d_grid_start = nullptr;      /* [G+1] */
+    uint32_t *d_grid_cursor = nullptr;     /* [G] */
+    uint32_t *d_sorted = nullptr;          /* [N] */
+    uint32_t *d_rank_of = nullptr;         /* [N] sorted position of each object */
+    double2 *d_sxy = nullptr;
+    double *d_sL = nullptr;
+    uint32_t *d_leaf_work = nullptr;       /* [G] grid ids with objects */
+
+    /* schema */
+    glint::DNode *d_nodes = nullptr;
+    double2 *d_low = nullptr;
+    uint32_t *d_sstack = nullptr;
+    uint32_t *d_gstack = nullptr;
+    uint8_t *d_split = nullptr;            /* [S] per-slot event flags */
+    uint32_t *d_evscan = nullptr;          /* [S] candidate leaf-children sums */
+    uint32_t *d_cand = nullptr;            /* [S] merge candidates */
+    uint32_t *d_newgid = nullptr;          /* [S] grid id a merged node takes */
+    uint32_t *d_events = nullptr;          /* [S+1] per-slot event indicator */
+    uint32_t *d_evpos = nullptr;           /* [S+1] its exclusive scan */
+    uint32_t *d_evlist = nullptr;          /* [S] event slots in slot order */
+    uint4 *d_evdata = nullptr;             /* [2S] per-event replay data */
+    int32_t *d_evlevel = nullptr;          /* [S] stack level before each event */
+    uint32_t *d_big = nullptr;             /* [G] leaves sorted by a whole block */
+
+    /* filter */
+    uint32_t *d_qcount = nullptr, *d_qstart = nullptr, *d_qlist = nullptr;
+    uint32_t *d_qtmp = nullptr;            /* [N*8] first targets of each border object */
+    uint32_t *d_tcount = nullptr, *d_tstart = nullptr, *d_tcursor = nullptr;
+    uint2 *d_tlist = nullptr;
+
+    /* table */
+    glint::TRec *d_tab = nullptr;
+    uint8_t *d_stamp = nullptr;
+    glint::NewEntry *d_new = nullptr;
+    uint32_t *d_tile_cnt = nullptr, *d_tile_off = nullptr;
+    uint64_t n_tiles = 0;
+
+    /* output */
+    glint_meeting *d_log = nullptr;
+
+    /* misc */
+    glint::DevCounters *d_cnt = nullptr;
+    glint::DevCounters *h_cnt = nullptr;   /* pinned */
+    glint::SinCoef *d_coef = nullptr;
+    void *d_scan_tmp = nullptr;
+    size_t scan_tmp_bytes = 0;
+    double2 *h_stage = nullptr;            /* pinned staging for host points (optional) */
+    glint::StepTimers timers;
+    glint_step_stats last_stats;
+    bool stats_valid = false;
+};
+
+namespace glint {
+
+/* ---- utilities (k_util.cu) ---- */
+size_t scan_tmp_bytes(size_t n);
+/* exclusive scan of n u32 values into out[0..n], out[n] = total */
+cudaError_t scan_u32(const uint32_t *in, uint32_t *out, size_t n, void *tmp, cudaStream_t s);
+void init_sin_coef(SinCoef *host);
+
+/* ---- stages ---- */
+cudaError_t launch_partition(glint_ctx *c, uint32_t cur_time);
+cudaError_t launch_filter(glint_ctx *c);
+cudaError_t launch_refine(glint_ctx *c, uint32_t cur_time);
+cudaError_t launch_insert(glint_ctx *c, uint32_t cur_time);
+cudaError_t launch_identify(glint_ctx *c, uint32_t cur_time);
+cudaError_t launch_schema_update(glint_ctx *c);
+
+inline ExactCtx make_exact(glint_ctx *c) {
+    ExactCtx e;
+    e.r = c->cfg.reach_distance;
+    e.dpm_lat = c->dpm_lat;
+    e.band = c->band;
+    e.coef = c->d_coef;
+    e.ambiguous = &c->d_cnt->ambiguous;
+    e.rechecks = &c->d_cnt->rechecks;
+    return e;
+}
+
+inline unsigned int grid_for(uint64_t n, unsigned int block, unsigned int cap = 152u * 32u) {
+    uint64_t g = (n + block - 1) / block;
+    if (g == 0) g = 1;
+    if (g > cap) g = cap;
+    return (unsigned int)g;
+}
+
+} // namespace glint
+
+#endif

@@ -1,0 +1,217 @@
+/*
+ * glint.h -- C ABI of the GB300-native GLINT contact-tracing step.
+ *
+ * This is the drop-in boundary for the reference's per-timestep GPU seam:
+ *
+ *   workbench *cuda_create_device_bench(workbench *bench, gpu_info *gpu);
+ *       declared tracing/process.cpp:373-374, defined cuda/geometry.cu:1395-1565
+ *       -> glint_create()
+ *   void process_with_gpu(workbench *bench, workbench *d_bench, gpu_info *gpu);
+ *       declared tracing/process.cpp:375, defined cuda/geometry.cu:1573-2218,
+ *       called once per timestep at tracing/process.cpp:462
+ *       -> glint_step() / glint_step_device()
+ *
+ * and, on the CPU side, for workbench::filter / reachability /
+ * update_meetings / update_schema (tracing/workbench.h:311-313, 339), whose
+ * results (the meetings identified each step, tracing/meeting.cpp:11-24) are
+ * returned by glint_meetings().  The flush of finished meetings into the
+ * sorted key-value + bitmap store (cuda/geometry.cu:1752-2135,
+ * tracing/step_merge.cpp:132-186) is glint_flush(); contact-trace queries
+ * against that store are glint_query_*().
+ *
+ * Plain pointers and sizes only.  Every call returns a status instead of
+ * exiting (the reference's CUDA_SAFE_CALL exits, cuda/cuda_util.cuh:19-27).
+ * A context owns its CUDA stream and device memory; input buffers are
+ * borrowed for the duration of a call.  One context per host thread.
+ */
+#ifndef GLINT_H_
+#define GLINT_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GLINT_ABI_VERSION 1
+
+typedef enum glint_status {
+    GLINT_OK = 0,
+    GLINT_ERR_INVALID_ARGUMENT = 1,
+    GLINT_ERR_CUDA = 2,
+    GLINT_ERR_OUT_OF_MEMORY = 3,
+    GLINT_ERR_CAPACITY = 4,      /* a fixed-size device buffer overflowed; see error_flags */
+    GLINT_ERR_UNSUPPORTED = 5,
+    GLINT_ERR_STATE = 6,
+    GLINT_ERR_NO_DEVICE = 7
+} glint_status;
+
+/* error_flags bits (glint_step_stats.error_flags) */
+#define GLINT_EF_CHECKS_OVERFLOW     0x0001u /* cross-leaf check buffer full */
+#define GLINT_EF_NEW_OVERFLOW        0x0002u /* per-step new-contact buffer full */
+#define GLINT_EF_TABLE_FULL          0x0004u /* meeting table probe found no empty slot */
+#define GLINT_EF_LOG_OVERFLOW        0x0008u /* device meeting log full */
+#define GLINT_EF_SCHEMA_STACK        0x0010u /* schema or grid stack exhausted */
+#define GLINT_EF_SEGMENT_TOO_LARGE   0x0020u /* a leaf holds more objects than the sorter supports */
+#define GLINT_EF_DUPLICATE_NEW       0x0040u /* internal: a new key was inserted twice */
+#define GLINT_EF_DFS_OVERFLOW        0x0080u /* lookup depth beyond the supported tree depth */
+#define GLINT_EF_SCHEMA_WINDOW       0x0100u /* schema update took the slow path */
+#define GLINT_EF_TREE_DEPTH          0x0200u /* descent deeper than the supported tree depth */
+
+/* The configuration fields this path reads from the reference's
+ * `configuration` (util/config.h:15-114), plus this implementation's own. */
+typedef struct glint_config {
+    uint32_t num_objects;          /* configuration::num_objects */
+    uint32_t grid_capacity;        /* configuration::grid_capacity (50) */
+    double grid_amplify;           /* configuration::grid_amplify (2): leaf buffer = amplify*capacity */
+    uint64_t num_meeting_buckets;  /* configuration::num_meeting_buckets; 0 -> 2*num_objects (config.h:176-178) */
+    double reach_distance;         /* configuration::reach_distance, metres (2) */
+    uint32_t min_meet_time;        /* configuration::min_meet_time (5) */
+    uint32_t max_meet_time;        /* configuration::max_meet_time (4096) */
+    uint32_t schema_update_delay;  /* configuration::schema_update_delay (1) */
+    uint32_t dynamic_schema;       /* configuration::dynamic_schema (1) */
+    uint32_t phased_lookup;        /* configuration::phased_lookup; only 1 is supported */
+    uint32_t start_time;           /* configuration::start_time */
+    double x_buffer;               /* configuration::x_buffer; 0 -> reach*dpm_lon(mbr.low.y) (filter.cpp:30) */
+    double y_buffer;               /* configuration::y_buffer; 0 -> reach*dpm_lat (filter.cpp:31) */
+    uint32_t G_bytes;              /* configuration::G_bytes: kv_restriction = G_bytes*2^25 keys (config.h:77-85) */
+    uint32_t CTF_count;            /* configuration::CTF_count (100); must be a square */
+    double dProbFalse;             /* workbench::dProbFalse: object-box area above which keys go to the oversize buffer */
+    /* ---- this implementation ---- */
+    uint32_t precision_mode;       /* 0: FP64 test on every candidate; 1: FP32 leaf-relative guard band */
+    uint32_t device;               /* CUDA device ordinal */
+    uint64_t new_capacity;         /* per-step new-contact buffer (entries); 0 -> automatic */
+    uint64_t check_capacity;       /* cross-leaf check buffer (entries); 0 -> automatic */
+    uint64_t meeting_log_capacity; /* meetings kept on device until the next flush; 0 -> automatic */
+    uint32_t timing;               /* 1: record per-stage CUDA-event times in glint_step_stats.ms */
+    uint32_t auto_flush;           /* 1: flush when the log passes kv_restriction keys, as geometry.cu:1752 */
+    uint32_t reserved[6];
+} glint_config;
+
+typedef struct glint_box {
+    double low[2];                 /* lon, lat */
+    double high[2];
+} glint_box;
+
+/* Same field layout as the reference's QTSchema (index/QTree.h:49-62), 80 bytes,
+ * so a caller can pass workbench::schema unchanged. */
+typedef struct glint_schema_node {
+    uint32_t grid_id;
+    int16_t level;
+    int16_t type;                  /* 0 INVALID, 1 BRANCH, 2 LEAF */
+    int16_t overflow_count;
+    int16_t underflow_count;
+    double mid_x;
+    double mid_y;
+    double low[2];
+    double high[2];
+    uint32_t children[4];
+} glint_schema_node;
+
+/* an initial schema as partitioner::build_schema leaves it (filter.cpp:81-91) */
+typedef struct glint_schema_init {
+    const glint_schema_node *nodes;   /* workbench::schema, schema_stack_capacity records */
+    uint32_t num_nodes;               /* records in `nodes` */
+    uint32_t schema_stack_index;      /* workbench::schema_stack_index */
+    uint32_t grids_stack_index;       /* workbench::grids_stack_index */
+    uint32_t reserved;
+    const uint32_t *schema_stack;     /* NULL -> identity (workbench.cpp:106-112) */
+    const uint32_t *grids_stack;      /* NULL -> identity (workbench.cpp:95-100) */
+} glint_schema_init;
+
+/* one identified meeting: pid1 < pid2 (the Cantor pair key's ids), the
+ * first and last steps of contact, and the f32 box of both objects over it */
+typedef struct glint_meeting {
+    uint32_t pid1;
+    uint32_t pid2;
+    uint32_t start;
+    uint32_t end;
+    float mbr[4];                  /* low lon, low lat, high lon, high lat */
+} glint_meeting;
+
+typedef struct glint_step_stats {
+    uint32_t cur_time;
+    uint32_t checks;               /* inside + cross-leaf checks (grid_check_counter) */
+    uint32_t border_objects;       /* objects that ran the neighbour lookup (filter_list_index) */
+    uint32_t cross_checks;
+    uint64_t candidates;           /* distance tests evaluated */
+    uint64_t contacts;             /* distance tests within reach */
+    uint64_t new_keys;             /* contacts whose pair had no entry at the start of the step */
+    uint64_t num_taken_buckets;    /* occupied slots before expiry (meeting.cpp:136-139) */
+    uint32_t num_active_meetings;  /* entries touched this step (meeting.cpp:141-144) */
+    uint32_t meetings;             /* meetings identified this step */
+    uint32_t splits;
+    uint32_t merges;
+    uint32_t leaves;               /* grids_stack_index */
+    uint32_t nodes;                /* schema_stack_index */
+    uint32_t dropped_objects;      /* objects past a full leaf buffer (filter.cpp:102) */
+    uint32_t rechecks;             /* decisions re-taken with the correctly rounded sin */
+    uint32_t ambiguous;            /* rechecks whose outcome depended on libm's last bit */
+    uint32_t band_pairs;           /* precision mode: pairs inside the FP32 guard band */
+    uint32_t error_flags;          /* GLINT_EF_* */
+    uint32_t pad;
+    uint64_t meeting_log_size;     /* meetings held on device for the next flush */
+    float ms[8];                   /* copy, partition, filter, refine, insert, identify, schema, total */
+} glint_step_stats;
+
+typedef struct glint_ctx glint_ctx;
+
+int glint_abi_version(void);
+const char *glint_status_string(glint_status s);
+/* sizeof of glint_config, glint_box, glint_schema_node, glint_schema_init,
+ * glint_meeting and glint_step_stats, in that order (binding self-check) */
+void glint_struct_sizes(uint32_t out[6]);
+/* fills a config with the reference's defaults for n objects (util/config.h) */
+void glint_config_defaults(glint_config *cfg, uint32_t num_objects);
+
+/* cuda_create_device_bench: allocate device state and upload the initial
+ * schema.  `init` may be NULL, in which case the schema is built from
+ * first_points (N lon/lat pairs, host memory) with the reference's rule
+ * (index/QTree.h:157-185). */
+glint_status glint_create(const glint_config *cfg, const glint_box *mbr, const double *first_points,
+                          const glint_schema_init *init, glint_ctx **out);
+glint_status glint_destroy(glint_ctx *ctx);
+const char *glint_last_error(const glint_ctx *ctx);
+
+/* process_with_gpu: one timestep.  points = N (lon, lat) FP64 pairs in host
+ * memory, copied in on the context's stream; returns after the step
+ * completes, with stats (may be NULL). */
+glint_status glint_step(glint_ctx *ctx, const double *points, uint32_t cur_time, glint_step_stats *stats);
+/* the same with points already in device memory; enqueues the step on the
+ * context's stream and returns without waiting */
+glint_status glint_step_device(glint_ctx *ctx, const double *d_points, uint32_t cur_time);
+/* waits for enqueued steps; stats of the last one (may be NULL) */
+glint_status glint_sync(glint_ctx *ctx, glint_step_stats *stats);
+
+/* meetings identified by the last step, in bucket order (the order of
+ * workbench::h_meetings_ps, tracing/meeting.cpp:147-153); *n receives the count */
+glint_status glint_meetings(glint_ctx *ctx, glint_meeting *out, uint64_t cap, uint64_t *n);
+
+/* debugging / parity state: schema records (num_nodes), the free part of the
+ * two stacks, and per-grid object counts from the last step's filter */
+glint_status glint_get_schema(glint_ctx *ctx, glint_schema_node *nodes, uint32_t *schema_stack, uint32_t *grids_stack,
+                              uint32_t *grid_counter, uint32_t *schema_stack_index, uint32_t *grids_stack_index);
+/* table contents: key (or 1<<62 when empty) and start per bucket */
+glint_status glint_get_buckets(glint_ctx *ctx, uint64_t *keys, uint32_t *starts, float *mbrs);
+/* sizes the context was created with */
+glint_status glint_get_capacities(const glint_ctx *ctx, uint32_t *schema_capacity, uint32_t *grids_capacity,
+                                  uint64_t *buckets);
+/* the context's cudaStream_t */
+void *glint_stream(glint_ctx *ctx);
+
+/* ---- synthetic trajectories on the device (benchmark input) ----
+ * params/objects: the generator's parameter block and object states as
+ * produced by the host generator (glint_pipeline_gb300/csrc/tracegen.h) */
+typedef struct glint_gen glint_gen;
+glint_status glint_gen_create(const void *params, uint32_t params_size, const void *objects, uint32_t num_objects,
+                              uint32_t object_size, uint32_t first_step, glint_gen **out);
+/* advance to the next step and write N (lon, lat) pairs to d_out on `stream` */
+glint_status glint_gen_step(glint_gen *g, double *d_out, void *stream);
+glint_status glint_gen_destroy(glint_gen *g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GLINT_H_ */

@@ -1,0 +1,306 @@
+"""ctypes bindings for the test oracle (liboracle.so, the C restatement) and for
+the reference's own CPU stages built into _ref/libglintref.so.
+
+TEST INFRASTRUCTURE: imported only by tests/, __graft_entry__.smoke() and
+bench.py's cpu_baseline leg.  The product never imports this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ORACLE_SO = os.path.join(HERE, "liboracle.so")
+REF_SO = os.path.join(HERE, "_ref", "libglintref.so")
+REFERENCE_ROOT = os.environ.get("GLINT_REFERENCE_ROOT", "/root/reference")
+
+
+def build_oracle() -> str:
+    subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
+    return ORACLE_SO
+
+
+def build_ref() -> str | None:
+    """Builds the reference's own sources when they are present (this
+    container); returns None elsewhere."""
+    if not os.path.isdir(os.path.join(REFERENCE_ROOT, "src", "tracing")):
+        return None
+    subprocess.run(["sh", os.path.join(HERE, "build_ref.sh"), REFERENCE_ROOT], check=True,
+                   stdout=subprocess.DEVNULL)
+    return REF_SO
+
+
+class GoConfig(ctypes.Structure):
+    _fields_ = [
+        ("num_objects", ctypes.c_uint32),
+        ("grid_capacity", ctypes.c_uint32),
+        ("schema_update_delay", ctypes.c_uint32),
+        ("min_meet_time", ctypes.c_uint32),
+        ("dynamic_schema", ctypes.c_uint32),
+        ("pad0", ctypes.c_uint32),
+        ("num_meeting_buckets", ctypes.c_uint64),
+        ("grid_amplify", ctypes.c_double),
+        ("reach_distance", ctypes.c_double),
+    ]
+
+
+class GoCounts(ctypes.Structure):
+    _fields_ = [
+        ("grid_check_counter", ctypes.c_uint32),
+        ("kv_count", ctypes.c_uint32),
+        ("num_taken_buckets", ctypes.c_uint64),
+        ("num_active_meetings", ctypes.c_uint32),
+        ("grids_stack_index", ctypes.c_uint32),
+        ("schema_stack_index", ctypes.c_uint32),
+        ("grids_stack_capacity", ctypes.c_uint32),
+        ("schema_stack_capacity", ctypes.c_uint32),
+        ("grid_capacity", ctypes.c_uint32),
+        ("contacts", ctypes.c_uint64),
+        ("candidates", ctypes.c_uint64),
+        ("n_splits", ctypes.c_uint32),
+        ("n_merges", ctypes.c_uint32),
+        ("x_buffer", ctypes.c_double),
+        ("y_buffer", ctypes.c_double),
+    ]
+
+
+MEETING_DTYPE = np.dtype([("key", "<u8"), ("start", "<u4"), ("end", "<u4"), ("mbr", "<f4", (4,))])
+SCHEMA_DTYPE = np.dtype([
+    ("grid_id", "<u4"), ("level", "<i2"), ("type", "<i2"), ("overflow_count", "<i2"),
+    ("underflow_count", "<i2"), ("pad", "<u4"), ("mid_x", "<f8"), ("mid_y", "<f8"),
+    ("low", "<f8", (2,)), ("high", "<f8", (2,)), ("children", "<u4", (4,)),
+])
+assert SCHEMA_DTYPE.itemsize == 80
+
+
+def _load_oracle():
+    if not os.path.exists(ORACLE_SO):
+        build_oracle()
+    lib = ctypes.CDLL(ORACLE_SO)
+    vp = ctypes.c_void_p
+    lib.go_create.restype = vp
+    lib.go_create.argtypes = [ctypes.POINTER(GoConfig), vp, vp]
+    lib.go_destroy.argtypes = [vp]
+    lib.go_step.argtypes = [vp, vp, ctypes.c_uint32]
+    lib.go_get_counts.argtypes = [vp, ctypes.POINTER(GoCounts)]
+    lib.go_get_meetings.restype = ctypes.c_uint32
+    lib.go_get_meetings.argtypes = [vp, vp, ctypes.c_uint32]
+    lib.go_get_schema.argtypes = [vp, vp, vp, vp, vp]
+    lib.go_get_buckets.argtypes = [vp, vp, vp, vp, vp]
+    lib.go_dpm_lon.restype = ctypes.c_double
+    lib.go_dpm_lon.argtypes = [ctypes.c_double]
+    lib.go_sin_cr.restype = ctypes.c_double
+    lib.go_sin_cr.argtypes = [ctypes.c_double]
+    lib.go_cantor.restype = ctypes.c_uint64
+    lib.go_cantor.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+    return lib
+
+
+_ORACLE = None
+
+
+def oracle_lib():
+    global _ORACLE
+    if _ORACLE is None:
+        _ORACLE = _load_oracle()
+    return _ORACLE
+
+
+def make_config(num_objects, *, grid_capacity=50, schema_update_delay=1, min_meet_time=5, dynamic_schema=True,
+                num_meeting_buckets=None, grid_amplify=2.0, reach_distance=2.0) -> GoConfig:
+    return GoConfig(num_objects, grid_capacity, schema_update_delay, min_meet_time, int(bool(dynamic_schema)), 0,
+                    int(num_meeting_buckets if num_meeting_buckets is not None else 2 * num_objects),
+                    float(grid_amplify), float(reach_distance))
+
+
+class Oracle:
+    """Single-threaded CPU restatement of the reference's per-step stages."""
+
+    def __init__(self, cfg: GoConfig, mbr: np.ndarray, first_points: np.ndarray):
+        self.lib = oracle_lib()
+        self.cfg = cfg
+        self._mbr = np.ascontiguousarray(mbr, dtype=np.float64)
+        pts = np.ascontiguousarray(first_points, dtype=np.float64)
+        self.h = self.lib.go_create(ctypes.byref(cfg), self._mbr.ctypes.data, pts.ctypes.data)
+
+    def step(self, points: np.ndarray, cur_time: int):
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        self.lib.go_step(self.h, pts.ctypes.data, int(cur_time))
+
+    def counts(self) -> GoCounts:
+        c = GoCounts()
+        self.lib.go_get_counts(self.h, ctypes.byref(c))
+        return c
+
+    def meetings(self) -> np.ndarray:
+        c = self.counts()
+        out = np.zeros(max(c.kv_count, 1), dtype=MEETING_DTYPE)
+        n = self.lib.go_get_meetings(self.h, out.ctypes.data, out.shape[0])
+        return out[: min(n, out.shape[0])]
+
+    def schema(self):
+        c = self.counts()
+        sch = np.zeros(c.schema_stack_capacity, dtype=SCHEMA_DTYPE)
+        ss = np.zeros(c.schema_stack_capacity, dtype=np.uint32)
+        gs = np.zeros(c.grids_stack_capacity, dtype=np.uint32)
+        gc = np.zeros(c.grids_stack_capacity, dtype=np.uint32)
+        self.lib.go_get_schema(self.h, sch.ctypes.data, ss.ctypes.data, gs.ctypes.data, gc.ctypes.data)
+        return sch, ss, gs, gc
+
+    def buckets(self):
+        B = int(self.cfg.num_meeting_buckets)
+        k = np.zeros(B, np.uint64)
+        s = np.zeros(B, np.uint32)
+        e = np.zeros(B, np.uint32)
+        m = np.zeros((B, 4), np.float32)
+        self.lib.go_get_buckets(self.h, k.ctypes.data, s.ctypes.data, e.ctypes.data, m.ctypes.data)
+        return k, s, e, m
+
+    def close(self):
+        if self.h:
+            self.lib.go_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class RefConfig(ctypes.Structure):
+    _fields_ = [
+        ("num_objects", ctypes.c_uint32), ("num_threads", ctypes.c_uint32), ("grid_capacity", ctypes.c_uint32),
+        ("schema_update_delay", ctypes.c_uint32), ("min_meet_time", ctypes.c_uint32),
+        ("dynamic_schema", ctypes.c_uint32), ("num_meeting_buckets", ctypes.c_uint64),
+        ("grid_amplify", ctypes.c_double), ("reach_distance", ctypes.c_double),
+        ("start_time", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+    ]
+
+
+class RefCounts(ctypes.Structure):
+    _fields_ = [
+        ("grid_check_counter", ctypes.c_uint32), ("kv_count", ctypes.c_uint32),
+        ("num_taken_buckets", ctypes.c_uint64), ("num_active_meetings", ctypes.c_uint32),
+        ("grids_stack_index", ctypes.c_uint32), ("schema_stack_index", ctypes.c_uint32),
+        ("grids_stack_capacity", ctypes.c_uint32), ("schema_stack_capacity", ctypes.c_uint32),
+        ("grid_capacity", ctypes.c_uint32), ("x_buffer", ctypes.c_double), ("y_buffer", ctypes.c_double),
+        ("ms_filter", ctypes.c_double), ("ms_refine", ctypes.c_double), ("ms_meet", ctypes.c_double),
+        ("ms_schema", ctypes.c_double),
+    ]
+
+
+_REF = None
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_SO) or os.path.isdir(os.path.join(REFERENCE_ROOT, "src", "tracing"))
+
+
+def ref_lib():
+    global _REF
+    if _REF is None:
+        if not os.path.exists(REF_SO):
+            if build_ref() is None:
+                raise FileNotFoundError("reference build unavailable (no sources on this machine)")
+        lib = ctypes.CDLL(REF_SO)
+        vp = ctypes.c_void_p
+        lib.ref_create.restype = vp
+        lib.ref_create.argtypes = [ctypes.POINTER(RefConfig), vp, vp]
+        lib.ref_step.argtypes = [vp, vp, ctypes.c_uint32]
+        lib.ref_get_counts.argtypes = [vp, ctypes.POINTER(RefCounts)]
+        lib.ref_get_meetings.restype = ctypes.c_uint32
+        lib.ref_get_meetings.argtypes = [vp, vp, vp, vp, ctypes.c_uint32]
+        lib.ref_get_schema.argtypes = [vp, vp, vp, vp, vp]
+        lib.ref_get_buckets.argtypes = [vp, vp, vp, vp]
+        lib.ref_schema_record_size.restype = ctypes.c_uint32
+        lib.ref_dpm_lon.restype = ctypes.c_double
+        lib.ref_dpm_lon.argtypes = [ctypes.c_double]
+        lib.ref_destroy.argtypes = [vp]
+        _REF = lib
+    return _REF
+
+
+class Reference:
+    """The reference's own CPU stages (tracing/*.cpp), one step at a time."""
+
+    def __init__(self, cfg: GoConfig, mbr: np.ndarray, first_points: np.ndarray, num_threads: int = 1,
+                 start_time: int = 0):
+        self.lib = ref_lib()
+        self.cfg = cfg
+        rc = RefConfig(cfg.num_objects, num_threads, cfg.grid_capacity, cfg.schema_update_delay, cfg.min_meet_time,
+                       cfg.dynamic_schema, cfg.num_meeting_buckets, cfg.grid_amplify, cfg.reach_distance,
+                       start_time, 0)
+        self._mbr = np.ascontiguousarray(mbr, dtype=np.float64)
+        pts = np.ascontiguousarray(first_points, dtype=np.float64)
+        self.h = self.lib.ref_create(ctypes.byref(rc), self._mbr.ctypes.data, pts.ctypes.data)
+
+    def step(self, points: np.ndarray, cur_time: int):
+        pts = np.ascontiguousarray(points, dtype=np.float64)
+        self.lib.ref_step(self.h, pts.ctypes.data, int(cur_time))
+
+    def counts(self) -> RefCounts:
+        c = RefCounts()
+        self.lib.ref_get_counts(self.h, ctypes.byref(c))
+        return c
+
+    def meetings(self) -> np.ndarray:
+        c = self.counts()
+        n = max(c.kv_count, 1)
+        k = np.zeros(n, np.uint64)
+        s = np.zeros(n, np.uint32)
+        e = np.zeros(n, np.uint32)
+        got = self.lib.ref_get_meetings(self.h, k.ctypes.data, s.ctypes.data, e.ctypes.data, n)
+        got = min(got, n)
+        out = np.zeros(got, dtype=MEETING_DTYPE)
+        out["key"] = k[:got]
+        out["start"] = s[:got]
+        out["end"] = e[:got]
+        return out
+
+    def schema(self):
+        c = self.counts()
+        assert self.lib.ref_schema_record_size() == 80
+        sch = np.zeros(c.schema_stack_capacity, dtype=SCHEMA_DTYPE)
+        ss = np.zeros(c.schema_stack_capacity, dtype=np.uint32)
+        gs = np.zeros(c.grids_stack_capacity, dtype=np.uint32)
+        gc = np.zeros(c.grids_stack_capacity, dtype=np.uint32)
+        self.lib.ref_get_schema(self.h, sch.ctypes.data, ss.ctypes.data, gs.ctypes.data, gc.ctypes.data)
+        return sch, ss, gs, gc
+
+    def buckets(self):
+        B = int(self.cfg.num_meeting_buckets)
+        k = np.zeros(B, np.uint64)
+        s = np.zeros(B, np.uint32)
+        e = np.zeros(B, np.uint32)
+        self.lib.ref_get_buckets(self.h, k.ctypes.data, s.ctypes.data, e.ctypes.data)
+        return k, s, e
+
+    def close(self):
+        if self.h:
+            self.lib.ref_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def cantor_inverse(keys: np.ndarray):
+    """Exact (a, b) with key = (a+b)(a+b+1)/2 + b, vectorised."""
+    z = keys.astype(np.uint64)
+    w = np.floor((np.sqrt(8.0 * z.astype(np.float64) + 1) - 1) / 2).astype(np.uint64)
+    for _ in range(3):
+        over = w * (w + np.uint64(1)) // np.uint64(2) > z
+        w = np.where(over, w - np.uint64(1), w)
+        under = (w + np.uint64(1)) * (w + np.uint64(2)) // np.uint64(2) <= z
+        w = np.where(under, w + np.uint64(1), w)
+    t = w * (w + np.uint64(1)) // np.uint64(2)
+    b = (z - t).astype(np.uint64)
+    a = (w - b).astype(np.uint64)
+    return a.astype(np.uint32), b.astype(np.uint32)

@@ -1,0 +1,34 @@
+#!/bin/sh
+# Builds oracle/_ref/libglintref.so from the reference's own CPU sources where
+# they lie (never copied into this repository) plus oracle/ref_driver.cpp.
+# Test infrastructure only; the product never loads the result.
+#
+#   usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+#
+# Flags: -O2 -ffp-contract=off so that FP64 expressions are evaluated with one
+# rounding per operation on every host (GCC contracts a*b+c into an FMA by
+# default on aarch64; x86-64 without -mfma never does).  The Boost stub in
+# oracle/ref_stub stands in for the uninstalled program_options header, which
+# util/config.h includes but the CPU stages never call.
+set -eu
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${1:-/root/reference}
+SRC="$REF/src"
+OUT="$HERE/_ref"
+if [ ! -d "$SRC/tracing" ]; then
+    echo "reference sources not found under $SRC" >&2
+    exit 2
+fi
+CUDA_INC=${CUDA_HOME:-/usr/local/cuda}/include
+mkdir -p "$OUT"
+CXX=${CXX:-g++}
+FLAGS="-std=c++17 -O2 -ffp-contract=off -fPIC -w -I$HERE/ref_stub -I$SRC -I$CUDA_INC -pthread -fopenmp"
+objs=""
+for f in filter refinement meeting workbench step_merge analyze; do
+    $CXX $FLAGS -c "$SRC/tracing/$f.cpp" -o "$OUT/$f.o" &
+    objs="$objs $OUT/$f.o"
+done
+$CXX $FLAGS -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o" &
+wait
+$CXX -shared -o "$OUT/libglintref.so" $objs "$OUT/ref_driver.o" -pthread -fopenmp -lm
+echo "built $OUT/libglintref.so"

@@ -1,0 +1,113 @@
+/*
+ * glint_oracle.h -- CPU restatement of GLINT's per-timestep contact-tracing
+ * path, used ONLY as the test oracle (tests/, __graft_entry__.smoke() and
+ * bench.py's cpu_baseline leg).  The product never links or calls it.
+ *
+ * It restates, single-threaded, the reference's CPU stages:
+ *   schema build        tracing/filter.cpp:27-93, index/QTree.h:98-311
+ *   filter              tracing/filter.cpp:95-111, 130-152, 209-313
+ *   reachability        tracing/refinement.cpp:10-85
+ *   update_meetings     tracing/meeting.cpp:32-189
+ *   update_schema       tracing/filter.cpp:316-449
+ * and the GPU path's per-meeting f32 MBR rule (cuda/geometry.cu:82-96,
+ * 469-491), which the CPU path lacks but the key-value store needs.
+ *
+ * Parity pin: tests compare this restatement against the reference's own
+ * sources built into oracle/_ref (build_ref.sh) on seeded inputs, and against
+ * fixtures in tests/golden generated from that build.
+ */
+#ifndef GLINT_ORACLE_H_
+#define GLINT_ORACLE_H_
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct go_config {
+    uint32_t num_objects;
+    uint32_t grid_capacity;       /* configuration::grid_capacity (50) */
+    uint32_t schema_update_delay; /* configuration::schema_update_delay (1) */
+    uint32_t min_meet_time;       /* configuration::min_meet_time (5) */
+    uint32_t dynamic_schema;      /* configuration::dynamic_schema (1) */
+    uint32_t pad0;
+    uint64_t num_meeting_buckets; /* configuration::num_meeting_buckets (2N) */
+    double grid_amplify;          /* configuration::grid_amplify (2) */
+    double reach_distance;        /* configuration::reach_distance (2 m) */
+} go_config;
+
+/* same field layout as the reference's QTSchema (index/QTree.h:49-62), 80 bytes */
+typedef struct go_schema {
+    uint32_t grid_id;
+    int16_t level;
+    int16_t type;
+    int16_t overflow_count;
+    int16_t underflow_count;
+    double mid_x;
+    double mid_y;
+    double low[2];
+    double high[2];
+    uint32_t children[4];
+} go_schema;
+
+enum { GO_INVALID = 0, GO_BRANCH = 1, GO_LEAF = 2 };
+
+typedef struct go_meeting {
+    uint64_t key;                 /* Cantor pair of (min id, max id) */
+    uint32_t start;
+    uint32_t end;
+    float mbr[4];                 /* low x, low y, high x, high y (GPU rule) */
+} go_meeting;
+
+typedef struct go_counts {
+    uint32_t grid_check_counter;
+    uint32_t kv_count;            /* meetings identified by the last step */
+    uint64_t num_taken_buckets;
+    uint32_t num_active_meetings;
+    uint32_t grids_stack_index;
+    uint32_t schema_stack_index;
+    uint32_t grids_stack_capacity;
+    uint32_t schema_stack_capacity;
+    uint32_t grid_capacity;       /* leaf buffer size = grid_amplify*grid_capacity */
+    uint64_t contacts;            /* distance tests that passed in the last step */
+    uint64_t candidates;          /* distance tests evaluated in the last step */
+    uint32_t n_splits;            /* schema splits in the last step */
+    uint32_t n_merges;            /* schema merges in the last step */
+    double x_buffer;
+    double y_buffer;
+} go_counts;
+
+typedef struct go_ctx go_ctx;
+
+/* the reference's geographic helpers (util/util.h:57-70) */
+double go_dpm_lon(double latitude);
+double go_dpm_lat(void);
+uint64_t go_cantor(uint32_t a, uint32_t b);
+void go_cantor_inverse(uint64_t z, uint32_t *a, uint32_t *b);
+
+/* builds the initial schema from the first step's points, as
+ * partitioner::build_schema does; mbr4 = low x, low y, high x, high y */
+go_ctx *go_create(const go_config *cfg, const double *mbr4, const double *points_xy);
+void go_destroy(go_ctx *c);
+
+/* one timestep: filter, reachability, update_meetings, update_schema */
+int go_step(go_ctx *c, const double *points_xy, uint32_t cur_time);
+
+void go_get_counts(const go_ctx *c, go_counts *out);
+/* meetings identified by the last step in bucket order; returns the count */
+uint32_t go_get_meetings(const go_ctx *c, go_meeting *out, uint32_t cap);
+/* raw state for step-by-step comparisons */
+void go_get_schema(const go_ctx *c, go_schema *schema, uint32_t *schema_stack, uint32_t *grids_stack,
+                   uint32_t *grid_counter);
+void go_get_buckets(const go_ctx *c, uint64_t *keys, uint32_t *starts, uint32_t *ends, float *mbrs);
+
+/* correctly rounded sin on [0, pi/2] by a double-double Taylor series; used to
+ * check how often libm's sin differs from the correctly rounded value */
+double go_sin_cr(double x);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,180 @@
+"""CUDA path vs the CPU oracle, step by step, through the C ABI.
+
+Integer and index outputs must be bit-exact: the meetings identified each
+step (pair, start, end, in the reference's bucket order), the f32 meeting
+boxes, the check / candidate / contact / bucket counts, the schema records,
+both free stacks and the whole bucket table.  The golden fixtures (produced
+by the reference's own sources) are checked against the GPU directly too.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from glint_pipeline_gb300 import Configuration, DeviceBench
+from oracle.bindings import Oracle, cantor_inverse, make_config
+from workloads import CASES, case_config, digest, make_points
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+EF_INFO = 0x0100  # GLINT_EF_SCHEMA_WINDOW is informational
+
+
+def gpu_config(cfgd, **kw):
+    c = Configuration(num_objects=cfgd["num_objects"], grid_capacity=cfgd["grid_capacity"],
+                      grid_amplify=cfgd["grid_amplify"], num_meeting_buckets=cfgd["num_meeting_buckets"],
+                      reach_distance=cfgd["reach_distance"], min_meet_time=cfgd["min_meet_time"],
+                      schema_update_delay=cfgd["schema_update_delay"])
+    for k, v in kw.items():
+        setattr(c, k, v)
+    return c
+
+
+def compare_meetings(mo, mg, t):
+    a, b = cantor_inverse(mo["key"])
+    assert len(mg) == len(mo), f"step {t}: {len(mg)} meetings on GPU, {len(mo)} in the oracle"
+    np.testing.assert_array_equal(mg["pid1"], a, err_msg=f"step {t} pid1")
+    np.testing.assert_array_equal(mg["pid2"], b, err_msg=f"step {t} pid2")
+    np.testing.assert_array_equal(mg["start"], mo["start"], err_msg=f"step {t} start")
+    np.testing.assert_array_equal(mg["end"], mo["end"], err_msg=f"step {t} end")
+    np.testing.assert_array_equal(mg["mbr"].view(np.uint32), mo["mbr"].view(np.uint32), err_msg=f"step {t} mbr")
+
+
+def compare_state(o, g):
+    c = o.counts()
+    sch_o, ss_o, gs_o, gc_o = o.schema()
+    sch_g, ss_g, gs_g, gc_g, ssi, gsi = g.schema()
+    assert (ssi, gsi) == (c.schema_stack_index, c.grids_stack_index)
+    np.testing.assert_array_equal(sch_g["type"], sch_o["type"])
+    v = sch_o["type"] != 0
+    for f in ("grid_id", "level", "mid_x", "mid_y", "low", "high", "overflow_count", "underflow_count"):
+        np.testing.assert_array_equal(sch_g[f][v], sch_o[f][v], err_msg=f)
+    br = sch_o["type"] == 1
+    np.testing.assert_array_equal(sch_g["children"][br], sch_o["children"][br])
+    np.testing.assert_array_equal(ss_g[ssi:], ss_o[ssi:])
+    np.testing.assert_array_equal(gs_g[gsi:], gs_o[gsi:])
+    np.testing.assert_array_equal(gc_g, gc_o)
+    ko, so, eo, mo = o.buckets()
+    kg, sg, mg = g.buckets()
+    np.testing.assert_array_equal(kg, ko)
+    occ = ko != (1 << 62)
+    np.testing.assert_array_equal(sg[occ], so[occ])
+    np.testing.assert_array_equal(mg[occ].view(np.uint32), mo[occ].view(np.uint32))
+
+
+def run_parity(name, steps=None, state_every=10, precision_mode=0):
+    box, pts = make_points(name, steps)
+    cfgd = case_config(name)
+    o = Oracle(make_config(**cfgd), box, pts[0])
+    g = DeviceBench(gpu_config(cfgd, precision_mode=precision_mode), box, pts[0])
+    compare_state(o, g)
+    total = 0
+    for t in range(pts.shape[0]):
+        o.step(pts[t], t)
+        st = g.step(pts[t], t)
+        c = o.counts()
+        assert st.error_flags & ~EF_INFO == 0, f"step {t}: error flags {st.error_flags:#x}"
+        assert st.ambiguous == 0
+        assert (st.checks, st.candidates, st.contacts) == (c.grid_check_counter, c.candidates, c.contacts), f"step {t}"
+        assert (st.num_taken_buckets, st.num_active_meetings) == (c.num_taken_buckets, c.num_active_meetings)
+        assert (st.nodes, st.leaves) == (c.schema_stack_index, c.grids_stack_index), f"step {t}"
+        compare_meetings(o.meetings(), g.meetings(), t)
+        total += st.meetings
+        if state_every and (t % state_every == state_every - 1 or t == pts.shape[0] - 1):
+            compare_state(o, g)
+    g.close()
+    o.close()
+    return total
+
+
+@pytest.mark.parametrize("name", ["dense_20k", "collide_20k", "skew_5k", "delay_10k", "reach_8k"])
+def test_parity_with_oracle(name):
+    assert run_parity(name) > 0
+
+
+def test_parity_small_100k():
+    """BASELINE configs[0] (100k objects, 100 steps) against the oracle."""
+    run_parity("small_100k", state_every=50)
+
+
+@pytest.mark.parametrize("name", sorted(CASES))
+def test_gpu_matches_reference_fixtures(name):
+    """The GPU's per-step meetings hash to the reference's (tests/golden)."""
+    gold = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    box, pts = make_points(name)
+    cfgd = case_config(name)
+    g = DeviceBench(gpu_config(cfgd), box, pts[0])
+    from glint_pipeline_gb300._abi import MEETING_DTYPE  # noqa: F401
+    from oracle.bindings import oracle_lib
+    lib = oracle_lib()
+    for t in range(pts.shape[0]):
+        st = g.step(pts[t], t)
+        m = g.meetings()
+        keys = np.array([lib.go_cantor(int(a), int(b)) for a, b in zip(m["pid1"], m["pid2"])], dtype=np.uint64)
+        assert digest(keys, m["start"], m["end"]) == str(gold["step_digests"][t]), f"{name} step {t}"
+        assert (st.checks, st.meetings, st.num_taken_buckets, st.num_active_meetings, st.leaves, st.nodes) == \
+            tuple(int(v) for v in gold["counts"][t])
+    g.close()
+
+
+def test_device_generator_matches_host():
+    import ctypes
+    from glint_pipeline_gb300 import _abi
+    from glint_pipeline_gb300.tracegen import TraceGenerator
+    n = 50_000
+    host = TraceGenerator(0x5151, n)
+    ref = host.steps(25)
+    g2 = TraceGenerator(0x5151, n)
+    lib = _abi.lib()
+    pb = g2.params_bytes()
+    ob = g2.objects_bytes()
+    h = ctypes.c_void_p()
+    assert lib.glint_gen_create(pb, len(pb), ob, n, len(ob) // n, 0, ctypes.byref(h)) == 0
+    cudart = ctypes.CDLL("libcudart.so") if False else None  # noqa: F841
+    import glint_pipeline_gb300 as gp
+    bench_cfg = gp.Configuration(num_objects=n)
+    b = gp.DeviceBench(bench_cfg, host.box(), ref[0])  # owns a stream and device memory we can borrow
+    out = np.zeros((n, 2))
+    # generate into the bench's own input buffer through step_device: compare via a host copy
+    for t in range(25):
+        dptr = _device_buffer(n)
+        assert lib.glint_gen_step(h, ctypes.c_void_p(dptr.ptr), ctypes.c_void_p(b.stream)) == 0
+        dptr.copy_to_host(out, b.stream)
+        np.testing.assert_array_equal(out, ref[t], err_msg=f"step {t}")
+        dptr.free()
+    lib.glint_gen_destroy(h)
+    b.close()
+
+
+class _device_buffer:
+    """A raw cudaMalloc'd buffer through libcudart (test helper)."""
+
+    def __init__(self, n):
+        import ctypes
+        self.rt = _cudart()
+        p = ctypes.c_void_p()
+        assert self.rt.cudaMalloc(ctypes.byref(p), ctypes.c_size_t(16 * n)) == 0
+        self.ptr = p.value
+        self.n = n
+
+    def copy_to_host(self, out, stream):
+        import ctypes
+        assert self.rt.cudaDeviceSynchronize() == 0
+        assert self.rt.cudaMemcpy(out.ctypes.data_as(ctypes.c_void_p), ctypes.c_void_p(self.ptr),
+                                  ctypes.c_size_t(16 * self.n), 2) == 0
+
+    def free(self):
+        import ctypes
+        self.rt.cudaFree(ctypes.c_void_p(self.ptr))
+
+
+def _cudart():
+    import ctypes
+    import glob
+    for cand in ["libcudart.so", "libcudart.so.13"] + glob.glob("/usr/local/cuda/lib64/libcudart.so*"):
+        try:
+            return ctypes.CDLL(cand)
+        except OSError:
+            continue
+    raise OSError("libcudart not found")
