@@ -329,12 +329,18 @@ __global__ void __launch_bounds__(kStackThreads) k_sch_stacks(uint32_t *__restri
 __global__ void __launch_bounds__(256) k_sch_apply_merge(DNode *__restrict__ nodes, const uint8_t *__restrict__ flags,
                                                          const uint32_t *__restrict__ newgid,
                                                          const uint32_t *__restrict__ events, const uint4 *evdata,
-                                                         const DevCounters *cnt) {
+                                                         uint32_t *__restrict__ grid_count, const DevCounters *cnt) {
     const uint32_t E = cnt->n_events;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < E; i += gridDim.x * blockDim.x) {
         const uint4 a = evdata[2 * i];
         if (a.x == 0xffffffffu || (flags[events[i]] & 3) != kEvMerge) continue;
         const uint32_t g = events[i];
+        /* merge_node zeroes the counters of the grids it frees (filter.cpp:331) */
+        const uint4 cg = evdata[2 * i + 1];
+        grid_count[cg.x] = 0;
+        grid_count[cg.y] = 0;
+        grid_count[cg.z] = 0;
+        grid_count[cg.w] = 0;
         nodes[a.x].type = kInvalid;
         nodes[a.y].type = kInvalid;
         nodes[a.z].type = kInvalid;
@@ -349,12 +355,17 @@ __global__ void __launch_bounds__(256) k_sch_apply_merge(DNode *__restrict__ nod
 __global__ void __launch_bounds__(256) k_sch_apply_split(DNode *__restrict__ nodes, double2 *__restrict__ low,
                                                          const uint8_t *__restrict__ flags,
                                                          const uint32_t *__restrict__ events, const uint4 *evdata,
-                                                         const DevCounters *cnt) {
+                                                         uint32_t *__restrict__ grid_count, const DevCounters *cnt) {
     const uint32_t E = cnt->n_events;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < E; i += gridDim.x * blockDim.x) {
         const uint32_t p = events[i];
         if ((flags[p] & 3) != kEvSplit) continue;
         const uint4 cs = evdata[2 * i], gs = evdata[2 * i + 1];
+        /* split_node zeroes the counters of the children's grids (filter.cpp:359) */
+        grid_count[gs.x] = 0;
+        grid_count[gs.y] = 0;
+        grid_count[gs.z] = 0;
+        grid_count[gs.w] = 0;
         const DNode pn = nodes[p];
         const double2 pl = low[p];
         const double xhalf = __dsub_rn(pn.mid_x, pl.x);
@@ -412,8 +423,10 @@ cudaError_t launch_schema_update(glint_ctx *c) {
     k_sch_evdata<<<152, 256, 0, s>>>(c->d_nodes, c->d_split, c->d_newgid, c->d_evlist, c->d_evdata, c->d_cnt);
     k_sch_stacks<<<1, kStackThreads, schema_stack_smem(kWinCap), s>>>(c->d_sstack, c->d_gstack, S, c->G, c->d_evdata,
                                                                        c->d_evlevel, kWinCap, c->d_cnt);
-    k_sch_apply_merge<<<152, 256, 0, s>>>(c->d_nodes, c->d_split, c->d_newgid, c->d_evlist, c->d_evdata, c->d_cnt);
-    k_sch_apply_split<<<152, 256, 0, s>>>(c->d_nodes, c->d_low, c->d_split, c->d_evlist, c->d_evdata, c->d_cnt);
+    k_sch_apply_merge<<<152, 256, 0, s>>>(c->d_nodes, c->d_split, c->d_newgid, c->d_evlist, c->d_evdata,
+                                          c->d_grid_count, c->d_cnt);
+    k_sch_apply_split<<<152, 256, 0, s>>>(c->d_nodes, c->d_low, c->d_split, c->d_evlist, c->d_evdata,
+                                          c->d_grid_count, c->d_cnt);
     return cudaGetLastError();
 }
 
