@@ -90,13 +90,13 @@ class GlintStepStats(ctypes.Structure):
         ("ambiguous", ctypes.c_uint32),
         ("band_pairs", ctypes.c_uint32),
         ("error_flags", ctypes.c_uint32),
-        ("pad", ctypes.c_uint32),
+        ("launches", ctypes.c_uint32),
         ("meeting_log_size", ctypes.c_uint64),
         ("ms", ctypes.c_float * 8),
     ]
 
     def as_dict(self):
-        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("pad", "ms")}
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f != "ms"}
         d["ms"] = list(self.ms)
         return d
 

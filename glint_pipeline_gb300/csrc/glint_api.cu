@@ -23,6 +23,7 @@
 namespace glint {
 void partition_set_attributes();
 void refine_set_attributes(uint32_t cap);
+void refine_prec_set_attributes(uint32_t cap);
 void schema_set_attributes();
 size_t refine_smem_bytes(uint32_t cap);
 uint64_t identify_tiles(uint64_t B);
@@ -150,7 +151,7 @@ cudaError_t dalloc(T **p, size_t count) {
 __global__ void k_fill_empty(TRec *tab, uint64_t B) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < B; i += (uint64_t)gridDim.x * blockDim.x) {
         TRec r;
-        r.w0 = kEmptyKey;
+        r.w0 = kEmptyW0;
         r.w1 = 0;
         r.mbr[0] = r.mbr[1] = r.mbr[2] = r.mbr[3] = 0;
         tab[i] = r;
@@ -438,6 +439,7 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     k_iota<<<grid_for(N, 256, 152u * 8u), 256, 0, c->stream>>>(c->d_order, N);
     partition_set_attributes();
     refine_set_attributes(c->cap);
+    refine_prec_set_attributes(c->cap);
     schema_set_attributes();
     for (auto &ev : c->timers.ev) cudaEventCreate(&ev);
     c->timers.created = true;
@@ -530,6 +532,9 @@ static void fill_stats(glint_ctx *c, glint_step_stats *st) {
     st->ambiguous = h.ambiguous;
     st->band_pairs = h.band_pairs;
     st->error_flags = h.error_flags;
+    /* kernels per step: partition 9, filter 9, refine 1, insert 1,
+     * identify 6, schema update 11, tail 1 (scans count three each) */
+    st->launches = 9 + 9 + 1 + 1 + 6 + (c->cfg.dynamic_schema ? 11 : 0) + 1;
     st->meeting_log_size = h.log_head;
     if (c->cfg.timing) {
         for (int k = 0; k < 7; ++k) cudaEventElapsedTime(&st->ms[k], c->timers.ev[k], c->timers.ev[k + 1]);
@@ -633,7 +638,8 @@ glint_status glint_get_buckets(glint_ctx *c, uint64_t *keys, uint32_t *starts, f
         const uint64_t n = std::min<uint64_t>(chunk, c->B - b);
         cudaMemcpy(buf.data(), c->d_tab + b, sizeof(TRec) * n, cudaMemcpyDeviceToHost);
         for (uint64_t i = 0; i < n; ++i) {
-            if (keys) keys[b + i] = buf[i].w0;
+            const unsigned long long w0 = buf[i].w0;
+            if (keys) keys[b + i] = (w0 == kEmptyW0) ? kEmptyKey : cantor(pair_a(w0), pair_b(w0));
             if (starts) starts[b + i] = (uint32_t)buf[i].w1;
             if (mbrs)
                 for (int k = 0; k < 4; ++k) mbrs[4 * (b + i) + k] = fdec(buf[i].mbr[k]);

@@ -53,7 +53,11 @@ struct __align__(64) DNode {
 static_assert(sizeof(DNode) == 64, "DNode must be 64 bytes");
 
 /* ---- meeting-table record (32 bytes, one sector) ----
- * w0: key (committed), key|kNewFlag (inserted this step) or kEmptyKey
+ * The bucket of a pair (a < b) is cantorPairing(a, b) % B as in the
+ * reference (tracing/refinement.cpp:34-37); the record stores the pair itself
+ * instead of the Cantor key, which is equivalent and needs no inverse.
+ * w0: (a << 32) | b (committed), kNewFlag | (a << 32) | b (inserted this
+ *     step) or kEmptyW0
  * w1: start time (committed) or insertion priority (new)
  * mbr: order-preserving encodings of the f32 box (low x, low y, high x, high y) */
 struct __align__(32) TRec {
@@ -62,6 +66,14 @@ struct __align__(32) TRec {
     uint32_t mbr[4];
 };
 static_assert(sizeof(TRec) == 32, "TRec must be 32 bytes");
+constexpr unsigned long long kEmptyW0 = ~0ull;
+constexpr unsigned long long kPairMask = ~kNewFlag;
+
+__host__ __device__ inline unsigned long long pair_word(uint32_t a, uint32_t b) {
+    return ((unsigned long long)a << 32) | b;
+}
+__host__ __device__ inline uint32_t pair_a(unsigned long long w) { return (uint32_t)(w >> 32) & 0x7fffffffu; }
+__host__ __device__ inline uint32_t pair_b(unsigned long long w) { return (uint32_t)w; }
 
 __host__ __device__ inline uint32_t fenc(float f) {
     uint32_t u;
@@ -230,6 +242,29 @@ __device__ inline bool box_le_exact(double lx, double ly, double hx, double hy, 
     if (e.rechecks) atomicAdd(e.rechecks, 1u);
     if ((r0 != r1 || r0 != r2) && e.ambiguous) atomicAdd(e.ambiguous, 1u);
     return r0;
+}
+
+/* box::distance(p, true) <= r decided from the exact FP64 offsets the
+ * reference computes, scaled and squared in FP32: with iLf = 1/L (FP32) and
+ * iMf = 1/dpm_lat the FP32 square has a relative error below 2^-20, so
+ * outside [r2lo, r2hi] = r^2 (1 -+ 2^-16) the FP32 decision equals the
+ * reference's; inside it the decision is re-taken exactly. */
+struct FastBox {
+    float iMf;
+    float r2lo, r2hi;
+};
+
+__device__ inline bool box_le_fast(double lx, double ly, double hx, double hy, double px, double py, double Lfast,
+                                   float iLf, const FastBox &fb, const ExactCtx &e) {
+    if (px >= lx && px <= hx && py >= ly && py <= hy) return true;
+    double ax = __dsub_rn(fabs(__dsub_rn(px, __dmul_rn(__dadd_rn(lx, hx), 0.5))), __dmul_rn(__dsub_rn(hx, lx), 0.5));
+    double ay = __dsub_rn(fabs(__dsub_rn(py, __dmul_rn(__dadd_rn(ly, hy), 0.5))), __dmul_rn(__dsub_rn(hy, ly), 0.5));
+    const float fx = (float)(ax < 0.0 ? 0.0 : ax) * iLf;
+    const float fy = (float)(ay < 0.0 ? 0.0 : ay) * fb.iMf;
+    const float q = __fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy));
+    if (q < fb.r2lo) return true;
+    if (q > fb.r2hi) return false;
+    return box_le_exact(lx, ly, hx, hy, px, py, Lfast, e);
 }
 
 /* box::width(true) > two_r (geometry/geometry.h:166-172), exact */

@@ -18,6 +18,8 @@
  * twice: by querier (CSR over object ids, for the duplicate rule in refine)
  * and grouped by target leaf (for the refine tiles).
  */
+#include <cmath>
+
 #include "glint_internal.cuh"
 
 namespace glint {
@@ -29,7 +31,7 @@ constexpr int kStackMax = 64;
  * returns the number of leaves kept */
 template <class Emit>
 __device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const double2 *__restrict__ low, uint32_t start,
-                                       double px, double py, double Lp, const ExactCtx &ex, DevCounters *cnt,
+                                       double px, double py, double Lp, const FastBox &fb, const ExactCtx &ex, DevCounters *cnt,
                                        Emit emit) {
     uint32_t st_node[kStackMax];
     uint8_t st_next[kStackMax];
@@ -38,6 +40,7 @@ __device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const do
     st_next[0] = 0;
     sp = 1;
     uint32_t kept = 0;
+    const float iLf = (float)(1.0 / Lp);
     while (sp > 0) {
         const int top = sp - 1;
         const uint8_t i = st_next[top];
@@ -46,7 +49,7 @@ __device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const do
         const uint32_t ch = nodes[st_node[top]].child[i];
         const DNode n = nodes[ch];
         const double2 lo = low[ch];
-        if (box_le_exact(lo.x, lo.y, n.high_x, n.high_y, px, py, Lp, ex)) {
+        if (box_le_fast(lo.x, lo.y, n.high_x, n.high_y, px, py, Lp, iLf, fb, ex)) {
             if (n.type == kLeaf) {
                 if (py < lo.y || (py < n.high_y && px < lo.x)) {
                     emit(n.gid, kept);
@@ -70,7 +73,7 @@ __global__ void __launch_bounds__(128) k_filter_walk(const uint32_t *__restrict_
                                                      const uint32_t *__restrict__ obj_leaf,
                                                      const DNode *__restrict__ nodes, const double2 *__restrict__ low,
                                                      uint32_t *__restrict__ qcount, uint32_t *__restrict__ qtmp,
-                                                     ExactCtx ex, DevCounters *cnt) {
+                                                     FastBox fb, ExactCtx ex, DevCounters *cnt) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
         const uint32_t pid = sorted[i];
         const uint32_t lv = obj_lv[pid];
@@ -78,7 +81,7 @@ __global__ void __launch_bounds__(128) k_filter_walk(const uint32_t *__restrict_
         if (lv != obj_leaf[pid]) {
             const double2 p = pts[pid];
             uint32_t *row = qtmp + (size_t)pid * kQInline;
-            kept = lookup_walk(nodes, low, lv, p.x, p.y, L[pid], ex, cnt, [&](uint32_t gid, uint32_t k) {
+            kept = lookup_walk(nodes, low, lv, p.x, p.y, L[pid], fb, ex, cnt, [&](uint32_t gid, uint32_t k) {
                 if (k < kQInline) row[k] = gid;
             });
             atomicAdd(&cnt->border_objects, 1u);
@@ -92,7 +95,7 @@ __global__ void __launch_bounds__(128) k_filter_emit(uint32_t N, const double2 *
                                                      const DNode *__restrict__ nodes, const double2 *__restrict__ low,
                                                      const uint32_t *__restrict__ qstart,
                                                      const uint32_t *__restrict__ qtmp, uint32_t *__restrict__ qlist,
-                                                     uint32_t *__restrict__ tcount, uint64_t check_cap, ExactCtx ex,
+                                                     uint32_t *__restrict__ tcount, uint64_t check_cap, FastBox fb, ExactCtx ex,
                                                      DevCounters *cnt) {
     for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < N; pid += gridDim.x * blockDim.x) {
         const uint32_t b = qstart[pid], e = qstart[pid + 1];
@@ -110,7 +113,7 @@ __global__ void __launch_bounds__(128) k_filter_emit(uint32_t N, const double2 *
         }
         if (n > (uint32_t)kQInline) {
             const double2 p = pts[pid];
-            lookup_walk(nodes, low, obj_lv[pid], p.x, p.y, L[pid], ex, cnt, [&](uint32_t gid, uint32_t k) {
+            lookup_walk(nodes, low, obj_lv[pid], p.x, p.y, L[pid], fb, ex, cnt, [&](uint32_t gid, uint32_t k) {
                 if (k >= (uint32_t)kQInline && k < n) {
                     qlist[b + k] = gid;
                     atomicAdd(&tcount[gid], 1u);
@@ -141,15 +144,20 @@ cudaError_t launch_filter(glint_ctx *c) {
     cudaStream_t s = c->stream;
     const uint32_t N = c->N, G = c->G;
     ExactCtx ex = make_exact(c);
+    FastBox fb;
+    const double r2 = c->cfg.reach_distance * c->cfg.reach_distance;
+    fb.iMf = (float)(1.0 / c->dpm_lat);
+    fb.r2lo = (float)(r2 * (1.0 - std::ldexp(1.0, -16)));
+    fb.r2hi = (float)(r2 * (1.0 + std::ldexp(1.0, -16)));
     k_filter_walk<<<grid_for(N, 128, 152u * 16u), 128, 0, s>>>(c->d_sorted, N, c->d_pts, c->d_L, c->d_obj_lv,
                                                                  c->d_obj_leaf, c->d_nodes, c->d_low, c->d_qcount,
-                                                                 c->d_qtmp, ex, c->d_cnt);
+                                                                 c->d_qtmp, fb, ex, c->d_cnt);
     scan_u32(c->d_qcount, c->d_qstart, N, c->d_scan_tmp, s);
     cudaMemsetAsync(c->d_tcount, 0, sizeof(uint32_t) * (G + 1), s);
     cudaMemsetAsync(c->d_tcursor, 0, sizeof(uint32_t) * G, s);
     k_filter_emit<<<grid_for(N, 128, 152u * 16u), 128, 0, s>>>(N, c->d_pts, c->d_L, c->d_obj_lv, c->d_nodes, c->d_low,
                                                                  c->d_qstart, c->d_qtmp,
-                                                                 c->d_qlist, c->d_tcount, c->check_cap, ex, c->d_cnt);
+                                                                 c->d_qlist, c->d_tcount, c->check_cap, fb, ex, c->d_cnt);
     scan_u32(c->d_tcount, c->d_tstart, G, c->d_scan_tmp, s);
     k_filter_group<<<grid_for(N, 256, 152u * 8u), 256, 0, s>>>(N, c->d_qstart, c->d_qlist, c->d_tstart, c->d_tcursor,
                                                                 c->d_tlist, c->check_cap);

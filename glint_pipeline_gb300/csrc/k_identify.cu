@@ -9,24 +9,128 @@
  * (batch_meet, tracing/meeting.cpp:11-24).
  *
  * Device form: a stamp byte per bucket says empty / touched at this step /
- * touched at the previous step / inserted this step, so the scan reads one
- * byte per bucket and touches the 32-byte record only for entries that
- * change.  Pass 1 counts the emissions of each 4096-bucket tile, an exclusive
- * scan gives every tile its offset, and pass 2 writes the meetings in bucket
- * order into the device log, finalises this step's new entries (start = now,
- * f32 box of the pair's two points, geometry.cu:481-489) and clears the
- * expired ones.
+ * touched at the previous step, so the scan reads one byte per bucket and the
+ * 32-byte record only of entries that expire.  Pass 1 (16 buckets per thread)
+ * removes expired entries that are too short, marks the ones to report and
+ * counts them per 8192-bucket tile; an exclusive scan gives every tile its
+ * offset; pass 2 visits only tiles with reports and writes them in bucket
+ * order into the device meeting log, then removes those entries.
  */
 #include "glint_internal.cuh"
 
 namespace glint {
 
-constexpr int kIdThreads = 1024;
-constexpr int kIdItems = 4;
+constexpr int kIdThreads = 512;
+constexpr int kIdItems = 16;
 constexpr uint32_t kIdTile = kIdThreads * kIdItems;
+constexpr uint8_t kStampEmit = 4;
 
-__device__ inline uint32_t block_scan_excl(uint32_t v, uint32_t *ws, uint32_t &total) {
+__global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict__ stamp, TRec *__restrict__ tab,
+                                                             uint64_t B, uint8_t st_now, uint32_t cur_time,
+                                                             uint32_t min_plus1, uint32_t *__restrict__ tile_cnt,
+                                                             const double2 *__restrict__ pts, uint32_t N,
+                                                             DevCounters *cnt) {
+    __shared__ uint32_t red[3][kIdThreads / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * kIdTile + (uint64_t)threadIdx.x * kIdItems;
+    uint32_t emit = 0, taken = 0, active = 0;
+    if (base < B) {
+        uint4 s4 = *reinterpret_cast<const uint4 *>(stamp + base); /* B is padded to a multiple of 16 */
+        uint32_t w[4] = {s4.x, s4.y, s4.z, s4.w};
+        bool changed = false;
+#pragma unroll
+        for (int k = 0; k < kIdItems; ++k) {
+            const uint32_t sh = 8 * (k & 3);
+            const uint8_t sv = (uint8_t)(w[k >> 2] >> sh);
+            if (sv == kStampEmpty || base + k >= B) continue;
+            ++taken;
+            if (sv == st_now) {
+                ++active;
+                continue;
+            }
+            TRec &r = tab[base + k];
+            if (sv == kStampNew) {
+                /* a pair inserted this step: start = now and the f32 box of
+                 * its two points (geometry.cu:481-489) */
+                ++active;
+                const unsigned long long pw = r.w0 & kPairMask;
+                const uint32_t pa = pair_a(pw), pb = pair_b(pw);
+                TRec nr;
+                nr.w0 = pw;
+                nr.w1 = cur_time;
+                if (pa < N && pb < N) {
+                    const double2 A = pts[pa], Bp = pts[pb];
+                    const float ax = (float)A.x, ay = (float)A.y, bx = (float)Bp.x, by = (float)Bp.y;
+                    nr.mbr[0] = min(fenc(ax), fenc(bx));
+                    nr.mbr[1] = min(fenc(ay), fenc(by));
+                    nr.mbr[2] = max(fenc(ax), fenc(bx));
+                    nr.mbr[3] = max(fenc(ay), fenc(by));
+                } else {
+                    atomicOr(&cnt->error_flags, GLINT_EF_DUPLICATE_NEW);
+                    nr.mbr[0] = nr.mbr[1] = nr.mbr[2] = nr.mbr[3] = 0;
+                }
+                r = nr;
+                w[k >> 2] = (w[k >> 2] & ~(0xffu << sh)) | ((uint32_t)st_now << sh);
+                changed = true;
+                continue;
+            }
+            const uint32_t start = (uint32_t)r.w1;
+            if (cur_time - start >= min_plus1) {
+                ++emit;
+                w[k >> 2] = (w[k >> 2] & ~(0xffu << sh)) | ((uint32_t)kStampEmit << sh);
+            } else {
+                *reinterpret_cast<ulonglong2 *>(&r) = make_ulonglong2(kEmptyW0, 0ull);
+                w[k >> 2] &= ~(0xffu << sh);
+            }
+            changed = true;
+        }
+        if (changed) *reinterpret_cast<uint4 *>(stamp + base) = make_uint4(w[0], w[1], w[2], w[3]);
+    }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    for (int o = 16; o > 0; o >>= 1) {
+        emit += __shfl_down_sync(0xffffffffu, emit, o);
+        taken += __shfl_down_sync(0xffffffffu, taken, o);
+        active += __shfl_down_sync(0xffffffffu, active, o);
+    }
+    if (lane == 0) {
+        red[0][wid] = emit;
+        red[1][wid] = taken;
+        red[2][wid] = active;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t e = 0, t = 0, a = 0;
+        for (int i = 0; i < kIdThreads / 32; ++i) {
+            e += red[0][i];
+            t += red[1][i];
+            a += red[2][i];
+        }
+        tile_cnt[blockIdx.x] = e;
+        if (t) atomicAdd(&cnt->taken, (unsigned long long)t);
+        if (a) atomicAdd(&cnt->active, a);
+    }
+}
+
+__global__ void __launch_bounds__(kIdThreads) k_expire_emit(uint8_t *__restrict__ stamp, TRec *__restrict__ tab,
+                                                            uint64_t B, uint32_t cur_time,
+                                                            const uint32_t *__restrict__ tile_cnt,
+                                                            const uint32_t *__restrict__ tile_off,
+                                                            glint_meeting *__restrict__ log, uint64_t log_cap,
+                                                            const DevCounters *cnt) {
+    if (tile_cnt[blockIdx.x] == 0) return; /* uniform per block */
+    __shared__ uint32_t ws[kIdThreads / 32];
+    const uint64_t base = (uint64_t)blockIdx.x * kIdTile + (uint64_t)threadIdx.x * kIdItems;
+    uint32_t w[4] = {0, 0, 0, 0};
+    uint32_t mine = 0;
+    if (base < B) {
+        uint4 s4 = *reinterpret_cast<const uint4 *>(stamp + base);
+        w[0] = s4.x; w[1] = s4.y; w[2] = s4.z; w[3] = s4.w;
+#pragma unroll
+        for (int k = 0; k < kIdItems; ++k)
+            if ((uint8_t)(w[k >> 2] >> (8 * (k & 3))) == kStampEmit) mine |= 1u << k;
+    }
+    /* block exclusive scan of the per-thread report counts */
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t v = (uint32_t)__popc(mine);
     uint32_t x = v;
     for (int o = 1; o < 32; o <<= 1) {
         uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
@@ -35,138 +139,37 @@ __device__ inline uint32_t block_scan_excl(uint32_t v, uint32_t *ws, uint32_t &t
     if (lane == 31) ws[wid] = x;
     __syncthreads();
     if (wid == 0) {
-        uint32_t s = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0u;
+        uint32_t s = lane < kIdThreads / 32 ? ws[lane] : 0u;
         for (int o = 1; o < 32; o <<= 1) {
             uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
             if (lane >= o) s += y;
         }
-        ws[lane] = s;
+        if (lane < kIdThreads / 32) ws[lane] = s;
     }
     __syncthreads();
-    uint32_t pre = (wid ? ws[wid - 1] : 0u) + x - v;
-    total = ws[(blockDim.x >> 5) - 1];
-    __syncthreads();
-    return pre;
-}
-
-__global__ void __launch_bounds__(kIdThreads) k_identify_count(const uint8_t *__restrict__ stamp,
-                                                               const TRec *__restrict__ tab, uint64_t B,
-                                                               uint8_t st_now, uint32_t cur_time, uint32_t min_plus1,
-                                                               uint32_t *__restrict__ tile_cnt, DevCounters *cnt) {
-    __shared__ uint32_t ws[32];
-    const uint64_t base = (uint64_t)blockIdx.x * kIdTile + (uint64_t)threadIdx.x * kIdItems;
-    uint32_t emit = 0, taken = 0, active = 0;
-    uint32_t st4 = 0;
-    if (base + kIdItems <= B) st4 = *reinterpret_cast<const uint32_t *>(stamp + base);
-    else
-        for (int k = 0; k < kIdItems; ++k)
-            if (base + k < B) st4 |= (uint32_t)stamp[base + k] << (8 * k);
-#pragma unroll
-    for (int k = 0; k < kIdItems; ++k) {
-        const uint8_t sv = (uint8_t)(st4 >> (8 * k));
-        if (sv == kStampEmpty) continue;
-        ++taken;
-        if (sv == kStampNew || sv == st_now) {
-            ++active;
-            continue;
-        }
-        const uint32_t start = (uint32_t)tab[base + k].w1;
-        if (cur_time - start >= min_plus1) ++emit;
-    }
-    uint32_t tot_e, tot_t, tot_a;
-    block_scan_excl(emit, ws, tot_e);
-    block_scan_excl(taken, ws, tot_t);
-    block_scan_excl(active, ws, tot_a);
-    if (threadIdx.x == 0) {
-        tile_cnt[blockIdx.x] = tot_e;
-        if (tot_t) atomicAdd(&cnt->taken, (unsigned long long)tot_t);
-        if (tot_a) atomicAdd(&cnt->active, tot_a);
-    }
-}
-
-__global__ void __launch_bounds__(kIdThreads) k_identify_write(uint8_t *__restrict__ stamp, TRec *__restrict__ tab,
-                                                               uint64_t B, uint8_t st_now, uint32_t cur_time,
-                                                               uint32_t min_plus1, const uint32_t *__restrict__ tile_off,
-                                                               const double2 *__restrict__ pts,
-                                                               glint_meeting *__restrict__ log, uint64_t log_cap,
-                                                               uint32_t N, DevCounters *cnt) {
-    __shared__ uint32_t ws[32];
-    const uint64_t base = (uint64_t)blockIdx.x * kIdTile + (uint64_t)threadIdx.x * kIdItems;
-    uint32_t st4 = 0;
-    if (base + kIdItems <= B) st4 = *reinterpret_cast<const uint32_t *>(stamp + base);
-    else
-        for (int k = 0; k < kIdItems; ++k)
-            if (base + k < B) st4 |= (uint32_t)stamp[base + k] << (8 * k);
-    uint32_t emit_mask = 0;
-    uint32_t starts[kIdItems];
-#pragma unroll
-    for (int k = 0; k < kIdItems; ++k) {
-        starts[k] = 0;
-        const uint8_t sv = (uint8_t)(st4 >> (8 * k));
-        if (sv == kStampEmpty || sv == st_now || sv == kStampNew) continue;
-        starts[k] = (uint32_t)tab[base + k].w1;
-        if (cur_time - starts[k] >= min_plus1) emit_mask |= 1u << k;
-    }
-    uint32_t tot;
-    uint32_t pos = block_scan_excl((uint32_t)__popc(emit_mask), ws, tot) + tile_off[blockIdx.x];
+    if (!mine) return;
+    uint32_t pos = tile_off[blockIdx.x] + (wid ? ws[wid - 1] : 0u) + x - v;
     const unsigned long long head = cnt->log_head;
-    uint32_t new_st4 = st4;
-    bool changed = false;
-#pragma unroll
     for (int k = 0; k < kIdItems; ++k) {
-        const uint8_t sv = (uint8_t)(st4 >> (8 * k));
-        const uint64_t slot = base + k;
-        if (sv == kStampEmpty || sv == st_now) continue;
-        changed = true;
-        if (sv == kStampNew) {
-            /* finalise an entry inserted this step */
-            const unsigned long long key = tab[slot].w0 & kKeyMask;
-            uint32_t pa, pb;
-            cantor_inverse(key, pa, pb);
-            if (pa >= N || pb >= N) {
-                atomicOr(&cnt->error_flags, GLINT_EF_DUPLICATE_NEW);
-                pa = pb = 0;
-            }
-            const double2 A = pts[pa], Bp = pts[pb];
-            const float ax = (float)A.x, ay = (float)A.y, bx = (float)Bp.x, by = (float)Bp.y;
-            TRec r;
-            r.w0 = key;
-            r.w1 = cur_time;
-            r.mbr[0] = min(fenc(ax), fenc(bx));
-            r.mbr[1] = min(fenc(ay), fenc(by));
-            r.mbr[2] = max(fenc(ax), fenc(bx));
-            r.mbr[3] = max(fenc(ay), fenc(by));
-            tab[slot] = r;
-            new_st4 = (new_st4 & ~(0xffu << (8 * k))) | ((uint32_t)st_now << (8 * k));
-            continue;
-        }
-        /* expire */
-        if (emit_mask & (1u << k)) {
-            const unsigned long long key = tab[slot].w0;
-            uint32_t pa, pb;
-            cantor_inverse(key, pa, pb);
-            const uint4 m = *reinterpret_cast<const uint4 *>(tab[slot].mbr);
-            glint_meeting out;
-            out.pid1 = pa;
-            out.pid2 = pb;
-            out.start = starts[k];
-            out.end = cur_time - 1;
-            out.mbr[0] = fdec(m.x);
-            out.mbr[1] = fdec(m.y);
-            out.mbr[2] = fdec(m.z);
-            out.mbr[3] = fdec(m.w);
-            log[(head + pos) % log_cap] = out;
-            ++pos;
-        }
-        tab[slot].w0 = kEmptyKey;
-        new_st4 &= ~(0xffu << (8 * k));
+        if (!(mine & (1u << k))) continue;
+        TRec &r = tab[base + k];
+        const unsigned long long w0 = r.w0;
+        const uint4 m = *reinterpret_cast<const uint4 *>(r.mbr);
+        glint_meeting out;
+        out.pid1 = pair_a(w0);
+        out.pid2 = pair_b(w0);
+        out.start = (uint32_t)r.w1;
+        out.end = cur_time - 1;
+        out.mbr[0] = fdec(m.x);
+        out.mbr[1] = fdec(m.y);
+        out.mbr[2] = fdec(m.z);
+        out.mbr[3] = fdec(m.w);
+        log[(head + pos) % log_cap] = out;
+        ++pos;
+        *reinterpret_cast<ulonglong2 *>(&r) = make_ulonglong2(kEmptyW0, 0ull);
+        w[k >> 2] &= ~(0xffu << (8 * (k & 3)));
     }
-    if (changed) {
-        if (base + kIdItems <= B) *reinterpret_cast<uint32_t *>(stamp + base) = new_st4;
-        else
-            for (int k = 0; k < kIdItems; ++k)
-                if (base + k < B) stamp[base + k] = (uint8_t)(new_st4 >> (8 * k));
-    }
+    *reinterpret_cast<uint4 *>(stamp + base) = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
 __global__ void k_identify_advance(const uint32_t *__restrict__ tile_off, uint64_t tiles, uint64_t log_cap,
@@ -178,20 +181,20 @@ __global__ void k_identify_advance(const uint32_t *__restrict__ tile_off, uint64
     if (total > log_cap) atomicOr(&cnt->error_flags, GLINT_EF_LOG_OVERFLOW);
 }
 
+uint64_t identify_tiles(uint64_t B) { return (B + kIdTile - 1) / kIdTile; }
+
 cudaError_t launch_identify(glint_ctx *c, uint32_t cur_time) {
     cudaStream_t s = c->stream;
-    const uint64_t tiles = (c->B + kIdTile - 1) / kIdTile;
+    const uint64_t tiles = identify_tiles(c->B);
     const uint8_t st_now = stamp_of(c->step_index);
     const uint32_t min_plus1 = c->cfg.min_meet_time + 1;
-    k_identify_count<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, st_now, cur_time, min_plus1,
-                                                            c->d_tile_cnt, c->d_cnt);
+    k_expire_count<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, st_now, cur_time, min_plus1,
+                                                          c->d_tile_cnt, c->d_pts, c->N, c->d_cnt);
     scan_u32(c->d_tile_cnt, c->d_tile_off, tiles, c->d_scan_tmp, s);
-    k_identify_write<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, st_now, cur_time, min_plus1,
-                                                            c->d_tile_off, c->d_pts, c->d_log, c->log_cap, c->N, c->d_cnt);
+    k_expire_emit<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, cur_time, c->d_tile_cnt,
+                                                         c->d_tile_off, c->d_log, c->log_cap, c->d_cnt);
     k_identify_advance<<<1, 1, 0, s>>>(c->d_tile_off, tiles, c->log_cap, c->d_cnt);
     return cudaGetLastError();
 }
-
-uint64_t identify_tiles(uint64_t B) { return (B + kIdTile - 1) / kIdTile; }
 
 } // namespace glint

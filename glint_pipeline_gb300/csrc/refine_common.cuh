@@ -1,0 +1,145 @@
+/*
+ * refine_common.cuh -- the contact queue shared by the refine kernels: pairs
+ * within reach are compacted with a warp ballot into a per-warp shared
+ * queue and applied to the meeting table 32 at a time.
+ */
+#ifndef GLINT_REFINE_COMMON_CUH_
+#define GLINT_REFINE_COMMON_CUH_
+
+#include "glint_internal.cuh"
+
+namespace glint {
+
+constexpr int kQueue = 64;
+constexpr uint32_t kProbeLimit = 1u << 22;
+
+struct QEntry {
+    unsigned long long pw;     /* pair word (a << 32) | b, a < b */
+    unsigned long long prio;   /* position in the reference's check order */
+    float x1, y1, x2, y2;      /* the two points, rounded to f32 */
+};
+
+struct RefineArgs {
+    const uint32_t *work;
+    const uint32_t *grid_start;
+    const uint32_t *grid_count;
+    const uint32_t *sorted;
+    const double2 *sxy;
+    const double *sL;
+    const uint32_t *tstart;
+    const uint2 *tlist;
+    const double2 *pts;
+    const double *L;
+    const uint32_t *obj_gid;
+    const uint32_t *rank_of;
+    const uint32_t *qstart;
+    const uint32_t *qlist;
+    const double2 *leaf_low;   /* per grid id: low corner of the leaf (precision form) */
+    TRec *tab;
+    uint8_t *stamp;
+    NewEntry *newlist;
+    uint64_t B, Bm, new_cap;
+    uint32_t cap;
+    uint8_t st;
+    ExactCtx ex;
+    DevCounters *cnt;
+};
+
+/* The table as it stood at the start of the step: keys do not change while
+ * the refine kernels run.  Found -> touch the entry (stamp, f32 box; each pair
+ * has at most one event per step, so the box needs no atomics).  Not found
+ * before an empty slot -> the pair is new this step. */
+__device__ inline bool table_touch(const RefineArgs &a, const QEntry &q) {
+    uint64_t slot = fastmod(cantor(pair_a(q.pw), pair_b(q.pw)), a.B, a.Bm);
+    for (uint32_t probe = 0; probe < kProbeLimit; ++probe) {
+        const unsigned long long w0 = a.tab[slot].w0;
+        if (w0 == q.pw) {
+            uint4 m = *reinterpret_cast<const uint4 *>(a.tab[slot].mbr);
+            const uint32_t lx = min(fenc(q.x1), fenc(q.x2)), hx = max(fenc(q.x1), fenc(q.x2));
+            const uint32_t ly = min(fenc(q.y1), fenc(q.y2)), hy = max(fenc(q.y1), fenc(q.y2));
+            if (lx < m.x || ly < m.y || hx > m.z || hy > m.w) {
+                m.x = min(m.x, lx);
+                m.y = min(m.y, ly);
+                m.z = max(m.z, hx);
+                m.w = max(m.w, hy);
+                *reinterpret_cast<uint4 *>(a.tab[slot].mbr) = m;
+            }
+            a.stamp[slot] = a.st;
+            return false;
+        }
+        if (w0 == kEmptyW0) return true;
+        slot = (slot + 1 == a.B) ? 0 : slot + 1;
+    }
+    atomicOr(&a.cnt->error_flags, GLINT_EF_TABLE_FULL);
+    return false;
+}
+
+/* warp-collective: process queue entries [0, n) one per lane */
+__device__ inline void drain_queue(const RefineArgs &a, QEntry *Q, uint32_t n) {
+    const int lane = threadIdx.x & 31;
+    for (uint32_t base = 0; base < n; base += 32) {
+        const uint32_t e = base + lane;
+        bool isnew = false;
+        QEntry q;
+        if (e < n) {
+            q = Q[e];
+            isnew = table_touch(a, q);
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, isnew);
+        if (m) {
+            unsigned long long off = 0;
+            const int leader = __ffs(m) - 1;
+            if (lane == leader) off = atomicAdd(&a.cnt->new_keys, (unsigned long long)__popc(m));
+            off = __shfl_sync(0xffffffffu, off, leader);
+            if (isnew) {
+                const unsigned long long idx = off + __popc(m & ((1u << lane) - 1u));
+                if (idx < a.new_cap) {
+                    a.newlist[idx].key = q.pw;
+                    a.newlist[idx].prio = q.prio;
+                } else {
+                    atomicOr(&a.cnt->error_flags, GLINT_EF_NEW_OVERFLOW);
+                }
+            }
+        }
+    }
+    __syncwarp();
+}
+
+/* warp-collective: append this lane's contact (if any) to the queue */
+__device__ inline void enqueue(const RefineArgs &a, QEntry *Q, uint32_t &qn, bool hit, unsigned long long pw,
+                               unsigned long long prio, float x1, float y1, float x2, float y2) {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, hit);
+    if (hit) {
+        QEntry &e = Q[qn + __popc(m & ((1u << lane) - 1u))];
+        e.pw = pw;
+        e.prio = prio;
+        e.x1 = x1;
+        e.y1 = y1;
+        e.x2 = x2;
+        e.y2 = y2;
+    }
+    qn += __popc(m);
+    __syncwarp();
+    if (qn >= 32) {
+        drain_queue(a, Q, 32);
+        const uint32_t rest = qn - 32;
+        if ((uint32_t)lane < rest) Q[lane] = Q[32 + lane];
+        __syncwarp();
+        qn = rest;
+    }
+}
+
+/* does object obj have a cross-leaf check on grid gid */
+__device__ inline bool has_check(const RefineArgs &a, uint32_t obj, uint32_t gid) {
+    const uint32_t b = a.qstart[obj], e = a.qstart[obj + 1];
+    for (uint32_t k = b; k < e; ++k)
+        if (a.qlist[k] == gid) return true;
+    return false;
+}
+
+__device__ inline unsigned long long pw_of(uint32_t p, uint32_t q) { return p < q ? pair_word(p, q) : pair_word(q, p); }
+
+} // namespace glint
+
+#endif

@@ -150,7 +150,7 @@ typedef struct glint_step_stats {
     uint32_t ambiguous;            /* rechecks whose outcome depended on libm's last bit */
     uint32_t band_pairs;           /* precision mode: pairs inside the FP32 guard band */
     uint32_t error_flags;          /* GLINT_EF_* */
-    uint32_t pad;
+    uint32_t launches;             /* kernels the step launched */
     uint64_t meeting_log_size;     /* meetings held on device for the next flush */
     float ms[8];                   /* copy, partition, filter, refine, insert, identify, schema, total */
 } glint_step_stats;

@@ -98,6 +98,12 @@ def test_parity_small_100k():
     run_parity("small_100k", state_every=50)
 
 
+@pytest.mark.parametrize("name", ["dense_20k", "collide_20k", "skew_5k", "reach_8k", "small_100k"])
+def test_parity_precision_form(name):
+    """FP32 guard-band refine: the same meetings, counts and state as the oracle."""
+    run_parity(name, state_every=25, precision_mode=1)
+
+
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_gpu_matches_reference_fixtures(name):
     """The GPU's per-step meetings hash to the reference's (tests/golden)."""
