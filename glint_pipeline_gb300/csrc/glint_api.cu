@@ -168,7 +168,7 @@ __global__ void k_step_tail(const uint32_t *qstart, uint32_t N, DevCounters *cnt
 }
 
 void free_all(glint_ctx *c) {
-    void *ptrs[] = {c->d_pts, c->d_L, c->d_obj_gid, c->d_obj_lv, c->d_obj_leaf, c->d_order, c->d_grid_count,
+    void *ptrs[] = {c->d_pts, c->d_sipos, c->d_sfpos, c->d_sc, c->d_fpos, c->d_ibox, c->d_obj_gid, c->d_obj_lv, c->d_obj_leaf, c->d_order, c->d_grid_count,
                     c->d_grid_start, c->d_grid_cursor, c->d_sorted, c->d_rank_of, c->d_sxy, c->d_sL, c->d_leaf_work,
                     c->d_nodes, c->d_low, c->d_sstack, c->d_gstack, c->d_split, c->d_evscan, c->d_cand, c->d_newgid,
                     c->d_events, c->d_evpos, c->d_evlist, c->d_evdata, c->d_evlevel, c->d_big, c->d_qcount,
@@ -183,14 +183,39 @@ void free_all(glint_ctx *c) {
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
-void to_device_nodes(const glint_schema_node *in, uint32_t n, std::vector<DNode> &dn, std::vector<double2> &lo) {
+/* the fixed-point frame: origin at the low corner of the map (widened to the
+ * root node's box), S = 2^k with the wider side spanning [2^39, 2^40) units */
+Frame make_frame(const glint_box &mbr, const glint_schema_node &root, double r, double dpm_lat) {
+    const double lx = std::min(mbr.low[0], root.low[0]), ly = std::min(mbr.low[1], root.low[1]);
+    const double hx = std::max(mbr.high[0], root.high[0]), hy = std::max(mbr.high[1], root.high[1]);
+    double ext = std::max(hx - lx, hy - ly);
+    if (!(ext > 0) || !std::isfinite(ext)) ext = 1.0;
+    int e = 0;
+    std::frexp(ext, &e); /* ext < 2^e */
+    const int k = std::min(48, std::max(0, 40 - e));
+    Frame f;
+    f.ox = std::isfinite(lx) ? lx : 0.0;
+    f.oy = std::isfinite(ly) ? ly : 0.0;
+    f.S = std::ldexp(1.0, k);
+    f.kdeg = (float)(kPIh / 180.0);
+    f.kc = (float)(40076000.0 / (360.0 * f.S));
+    f.cy = (float)(1.0 / (dpm_lat * f.S));
+    f.r2 = (float)(r * r);
+    f.band0 = (float)(64.0 * std::ldexp(1.0, -24) * r * r);
+    f.band1 = (float)(4.0 * r);
+    return f;
+}
+
+void to_device_nodes(const glint_schema_node *in, uint32_t n, const Frame &f, std::vector<DNode> &dn,
+                     std::vector<double2> &lo, std::vector<longlong4> &ib) {
     for (uint32_t i = 0; i < n; ++i) {
         DNode d;
         std::memset(&d, 0, sizeof(d));
-        d.mid_x = in[i].mid_x;
-        d.mid_y = in[i].mid_y;
-        d.high_x = in[i].high[0];
-        d.high_y = in[i].high[1];
+        d.kmx = dkey(in[i].mid_x);
+        d.kmy = dkey(in[i].mid_y);
+        d.khx = dkey(in[i].high[0]);
+        d.khy = dkey(in[i].high[1]);
+        ib[i] = fx_box(in[i].low[0], in[i].low[1], in[i].high[0], in[i].high[1], f);
         for (int k = 0; k < 4; ++k) d.child[k] = in[i].children[k];
         d.gid = in[i].grid_id;
         d.type = (uint8_t)in[i].type;
@@ -312,7 +337,10 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
         }                                                                  \
     } while (0)
     ALLOC(c->d_pts, N);
-    ALLOC(c->d_L, N);
+    ALLOC(c->d_sipos, N);
+    ALLOC(c->d_sfpos, N);
+    ALLOC(c->d_sc, N);
+    ALLOC(c->d_fpos, N);
     ALLOC(c->d_obj_gid, N);
     ALLOC(c->d_obj_lv, N);
     ALLOC(c->d_obj_leaf, N);
@@ -328,6 +356,7 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     ALLOC(c->d_big, G);
     ALLOC(c->d_nodes, S);
     ALLOC(c->d_low, S);
+    ALLOC(c->d_ibox, S);
     ALLOC(c->d_sstack, S);
     ALLOC(c->d_gstack, G);
     ALLOC(c->d_split, (size_t)S + 4);
@@ -418,11 +447,14 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
         delete c;
         return GLINT_ERR_UNSUPPORTED;
     }
+    c->frame = make_frame(*mbr, sch[0], cfg.reach_distance, c->dpm_lat);
     std::vector<DNode> dn(S);
     std::vector<double2> lo(S);
-    to_device_nodes(sch.data(), S, dn, lo);
+    std::vector<longlong4> ib(S);
+    to_device_nodes(sch.data(), S, c->frame, dn, lo, ib);
     cudaMemcpy(c->d_nodes, dn.data(), sizeof(DNode) * S, cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_low, lo.data(), sizeof(double2) * S, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_ibox, ib.data(), sizeof(longlong4) * S, cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_sstack, sstack.data(), sizeof(uint32_t) * S, cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_gstack, gstack.data(), sizeof(uint32_t) * G, cudaMemcpyHostToDevice);
     DevCounters hc;
@@ -613,12 +645,12 @@ glint_status glint_get_schema(glint_ctx *c, glint_schema_node *nodes, uint32_t *
             s.type = dn[i].type;
             s.overflow_count = dn[i].of;
             s.underflow_count = dn[i].uf;
-            s.mid_x = dn[i].mid_x;
-            s.mid_y = dn[i].mid_y;
+            s.mid_x = kdbl(dn[i].kmx);
+            s.mid_y = kdbl(dn[i].kmy);
             s.low[0] = lo[i].x;
             s.low[1] = lo[i].y;
-            s.high[0] = dn[i].high_x;
-            s.high[1] = dn[i].high_y;
+            s.high[0] = kdbl(dn[i].khx);
+            s.high[1] = kdbl(dn[i].khy);
             for (int k = 0; k < 4; ++k) s.children[k] = dn[i].child[k];
         }
     }

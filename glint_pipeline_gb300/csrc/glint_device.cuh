@@ -34,13 +34,46 @@ enum : uint8_t { kInvalid = 0, kBranch = 1, kLeaf = 2 }; /* index/QTree.h:43-47 
 enum : uint8_t { kStampEmpty = 0, kStampNew = 3 };
 __host__ __device__ inline uint8_t stamp_of(uint64_t step_index) { return (uint8_t)(1 + (step_index & 1)); }
 
+/* ---- exact comparisons without the FP64 pipe --------------------------------
+ * On sm_103a every FP64 instruction, compares and conversions included, issues
+ * at a small fraction of the FP32 rate, so the hot loops compare doubles as
+ * order-preserving 64-bit keys: for non-NaN doubles a < b exactly when
+ * dkey(a) < dkey(b) (-0 is folded onto +0, which IEEE compares equal). */
+__host__ __device__ inline uint64_t dbits(double d) {
+#if defined(__CUDA_ARCH__)
+    return (uint64_t)__double_as_longlong(d);
+#else
+    uint64_t b;
+    memcpy(&b, &d, 8);
+    return b;
+#endif
+}
+__host__ __device__ inline double bitsd(uint64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    double d;
+    memcpy(&d, &b, 8);
+    return d;
+#endif
+}
+__host__ __device__ inline uint64_t dkey(double d) {
+    uint64_t b = dbits(d);
+    if (b == 0x8000000000000000ull) b = 0;
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+__host__ __device__ inline double kdbl(uint64_t k) {
+    return bitsd((k >> 63) ? (k & 0x7fffffffffffffffull) : ~k);
+}
+
 /* ---- schema node as stored on the device (64 bytes, one half line) ----
  * The reference's QTSchema (index/QTree.h:49-62) is 80 bytes with the low
  * corner in the middle; the descent only needs mid, high, children and type,
- * so those share one 64-byte record and the low corner lives beside it. */
+ * so those share one 64-byte record (as comparison keys) and the low corner
+ * lives beside it. */
 struct __align__(64) DNode {
-    double mid_x, mid_y;
-    double high_x, high_y;
+    uint64_t kmx, kmy;   /* dkey(mid_x), dkey(mid_y) */
+    uint64_t khx, khy;   /* dkey(high_x), dkey(high_y) */
     uint32_t child[4];
     uint32_t gid;
     uint8_t type;
@@ -244,27 +277,105 @@ __device__ inline bool box_le_exact(double lx, double ly, double hx, double hy, 
     return r0;
 }
 
-/* box::distance(p, true) <= r decided from the exact FP64 offsets the
- * reference computes, scaled and squared in FP32: with iLf = 1/L (FP32) and
- * iMf = 1/dpm_lat the FP32 square has a relative error below 2^-20, so
- * outside [r2lo, r2hi] = r^2 (1 -+ 2^-16) the FP32 decision equals the
- * reference's; inside it the decision is re-taken exactly. */
-struct FastBox {
-    float iMf;
-    float r2lo, r2hi;
+/* ---- fixed-point frame for screening tests ----------------------------------
+ * Every coordinate is also held as a 64-bit integer X = rn((x - ox) * S) with
+ * S = 2^k (k chosen so the map spans about 2^40 units), so differences of
+ * coordinates are exact integers, each within 1 + 2^-12 units of the exact
+ * scaled difference.  A screening test converts the differences to FP32,
+ * scales them to metres with cx = 1/(L S) (L = degree_per_meter_longitude of
+ * the first point) and cy = 1/(dpm_lat S), and compares q = mx^2 + my^2 with
+ * r^2.  With u = 2^-24: cx is within 9u of exact (the FP64 angle rounded
+ * once, the rounded degree constant, sinf's 2 ulp and two products), so
+ * near the threshold
+ *   |q - d^2| <= 2 r (cx + cy) (1 + 2^-12) + 26 u r^2
+ * (integer rounding, then 23u from mx^2, 7u from my^2, 1u from the sum and
+ * the FP32 r^2 and band arithmetic).  The guard band is about twice that:
+ * 4 r (cx + cy) + 64 u r^2.  Outside the band the screening decision equals
+ * the reference's FP64 decision (whose own rounding is near 2^-50 relative);
+ * inside it the exact FP64 test decides.
+ * A coordinate farther than 2^60 units from the origin is clamped; the object
+ * then carries cx = NaN, which sends every test it takes part in to the exact
+ * path. */
+struct Frame {
+    double ox, oy;       /* map low corner */
+    double S;            /* units per degree, 2^k */
+    float kdeg;          /* fl32(kPI / 180) */
+    float kc;            /* fl32(40076000 / (360 S)): cx = sin(angle) * kc */
+    float cy;            /* metres per unit along y: 1/(dpm_lat S) */
+    float r2;            /* r^2 */
+    float band0;         /* 64 u r^2 */
+    float band1;         /* 4 r */
 };
 
-__device__ inline bool box_le_fast(double lx, double ly, double hx, double hy, double px, double py, double Lfast,
-                                   float iLf, const FastBox &fb, const ExactCtx &e) {
-    if (px >= lx && px <= hx && py >= ly && py <= hy) return true;
-    double ax = __dsub_rn(fabs(__dsub_rn(px, __dmul_rn(__dadd_rn(lx, hx), 0.5))), __dmul_rn(__dsub_rn(hx, lx), 0.5));
-    double ay = __dsub_rn(fabs(__dsub_rn(py, __dmul_rn(__dadd_rn(ly, hy), 0.5))), __dmul_rn(__dsub_rn(hy, ly), 0.5));
-    const float fx = (float)(ax < 0.0 ? 0.0 : ax) * iLf;
-    const float fy = (float)(ay < 0.0 ? 0.0 : ay) * fb.iMf;
-    const float q = __fadd_rn(__fmul_rn(fx, fx), __fmul_rn(fy, fy));
-    if (q < fb.r2lo) return true;
-    if (q > fb.r2hi) return false;
-    return box_le_exact(lx, ly, hx, hy, px, py, Lfast, e);
+constexpr double kFxLimit = 1152921504606846976.0; /* 2^60 */
+
+__host__ __device__ inline long long fx_coord(double v, double o, double S, bool *clamped) {
+    double t = (v - o) * S; /* S is a power of two: the product is exact */
+    bool c = false;
+    if (!(t < kFxLimit)) { t = kFxLimit; c = true; }
+    if (t < -kFxLimit) { t = -kFxLimit; c = true; }
+    if (clamped) *clamped = *clamped || c;
+#if defined(__CUDA_ARCH__)
+    return __double2ll_rn(t);
+#else
+    return llrint(t);
+#endif
+}
+
+/* metres per unit along x at latitude lat, FP32 (within 9u of exact) */
+__device__ inline float c_of_lat(double lat, const Frame &f) {
+    double a = fabs(lat);
+    if (a == 90.0) a = 89.0;
+    const float t = (float)__dsub_rn(90.0, a);
+    return sinf(t * f.kdeg) * f.kc;
+}
+
+/* the per-first-point screening limits */
+struct Screen {
+    float cx, lo, hi;
+};
+__device__ inline Screen make_screen(float cx, const Frame &f) {
+    const float band = f.band0 + f.band1 * (cx + f.cy);
+    Screen s;
+    s.cx = cx;
+    s.lo = f.r2 - band;
+    s.hi = f.r2 + band;
+    return s;
+}
+
+__device__ inline float fx_to_f(long long d) {
+    const long long lim = 1ll << 31;
+    return (d > -lim && d < lim) ? (float)(int)d : __ll2float_rn(d);
+}
+
+/* 1 within reach, 0 beyond, -1 inside the guard band (or a NaN scale);
+ * dx, dy in units */
+__device__ inline int fx_screen(long long dx, long long dy, const Screen &s, float cy) {
+    const float mx = fx_to_f(dx) * s.cx, my = fx_to_f(dy) * cy;
+    const float q = mx * mx + my * my;
+    if (q < s.lo) return 1;
+    if (q > s.hi) return 0;
+    return -1;
+}
+
+__host__ __device__ inline longlong4 fx_box(double lx, double ly, double hx, double hy, const Frame &f) {
+    longlong4 b;
+    b.x = fx_coord(lx, f.ox, f.S, nullptr);
+    b.y = fx_coord(ly, f.oy, f.S, nullptr);
+    b.z = fx_coord(hx, f.ox, f.S, nullptr);
+    b.w = fx_coord(hy, f.oy, f.S, nullptr);
+    return b;
+}
+
+/* box distance screening: the gap from the point to the box along each axis */
+__device__ inline int fx_box_screen(const longlong4 &b, long long px, long long py, const Screen &s, float cy) {
+    long long dx = b.x - px;
+    if (px - b.z > dx) dx = px - b.z;
+    if (dx < 0) dx = 0;
+    long long dy = b.y - py;
+    if (py - b.w > dy) dy = py - b.w;
+    if (dy < 0) dy = 0;
+    return fx_screen(dx, dy, s, cy);
 }
 
 /* box::width(true) > two_r (geometry/geometry.h:166-172), exact */

@@ -4,11 +4,14 @@
  *
  * HBM layout (N objects, G grid slots, S schema slots, B buckets):
  *   points      double2[N]   lon/lat as given, AoS 16 B per object
- *   L           double[N]    degree_per_meter_longitude(lat) with CUDA sin
  *   obj_*       u32[N]       leaf grid id, last_valid node, leaf node per object
  *   sorted      u32[N]       object ids sorted by (grid id, object id): leaf member lists
- *   sxy, sL     [N]          coordinates and L gathered in that order (leaf tiles)
- *   nodes       DNode[S]     64-byte schema records, low corners in low[S]
+ *   sxy         double2[N]   coordinates gathered in that order (leaf tiles)
+ *   sipos, sc   [N]          fixed-point coordinates (i64 pair) and screening scale, same order
+ *   sfpos, fpos float2[N]    FP32 coordinates (meeting boxes), sorted and by object id
+ *   sL          double[N]    degree_per_meter_longitude with CUDA sin (plain form only)
+ *   nodes       DNode[S]     64-byte schema records (comparison keys), low corners in
+ *                            low[S], fixed-point boxes in ibox[S]
  *   stacks      u32[S], u32[G]  free schema / grid slots (workbench.h:118-128)
  *   qlist/tlist              cross-leaf checks, by querier and by target leaf
  *   tab, stamp  TRec[B], u8[B]  the meeting table (32 B per bucket) and touch stamps
@@ -93,7 +96,6 @@ struct glint_ctx {
 
     /* objects */
     double2 *d_pts = nullptr;
-    double *d_L = nullptr;
     uint32_t *d_obj_gid = nullptr, *d_obj_lv = nullptr, *d_obj_leaf = nullptr;
     uint32_t *d_order = nullptr;           /* processing order of the descent */
     uint32_t *d_grid_count = nullptr;      /* [G+1] */
@@ -102,7 +104,13 @@ struct glint_ctx {
     uint32_t *d_sorted = nullptr;          /* [N] */
     uint32_t *d_rank_of = nullptr;         /* [N] sorted position of each object */
     double2 *d_sxy = nullptr;
-    double *d_sL = nullptr;
+    double *d_sL = nullptr;                /* [N] sorted L (plain form only) */
+    longlong2 *d_sipos = nullptr;          /* [N] sorted fixed-point coordinates */
+    float2 *d_sfpos = nullptr;             /* [N] sorted f32 coordinates (meeting boxes) */
+    float *d_sc = nullptr;                 /* [N] sorted metres per unit along x */
+    float2 *d_fpos = nullptr;              /* [N] f32 coordinates by object id */
+    longlong4 *d_ibox = nullptr;           /* [S] fixed-point node boxes */
+    glint::Frame frame;
     uint32_t *d_leaf_work = nullptr;       /* [G] grid ids with objects */
 
     /* schema */

@@ -27,12 +27,35 @@ namespace glint {
 constexpr int kQInline = 8;
 constexpr int kStackMax = 64;
 
+/* the querier of a walk: exact coordinates (for the top/right rule and the
+ * exact fallback), fixed-point coordinates and screening limits */
+struct WalkPoint {
+    double px, py;
+    uint64_t kx, ky;     /* dkey(px), dkey(py) */
+    long long X, Y;
+    Screen sc;
+};
+
+__device__ inline WalkPoint walk_point(const double2 p, const longlong2 ip, float c, const Frame &f) {
+    WalkPoint w;
+    w.px = p.x;
+    w.py = p.y;
+    w.kx = dkey(p.x);
+    w.ky = dkey(p.y);
+    w.X = ip.x;
+    w.Y = ip.y;
+    w.sc = make_screen(c, f);
+    return w;
+}
+
 /* lookup_rec from node `start`; calls emit(gid, ordinal) in walk order;
- * returns the number of leaves kept */
+ * returns the number of leaves kept.  The box test is screened on the
+ * fixed-point boxes; only a box within the guard band of the reach takes the
+ * reference's FP64 box distance. */
 template <class Emit>
-__device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const double2 *__restrict__ low, uint32_t start,
-                                       double px, double py, double Lp, const FastBox &fb, const ExactCtx &ex, DevCounters *cnt,
-                                       Emit emit) {
+__device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const double2 *__restrict__ low,
+                                       const longlong4 *__restrict__ ibox, uint32_t start, const WalkPoint &w,
+                                       const Frame &f, const ExactCtx &ex, DevCounters *cnt, Emit emit) {
     uint32_t st_node[kStackMax];
     uint8_t st_next[kStackMax];
     int sp = 0;
@@ -40,7 +63,7 @@ __device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const do
     st_next[0] = 0;
     sp = 1;
     uint32_t kept = 0;
-    const float iLf = (float)(1.0 / Lp);
+    double Lp = 0.0; /* degree_per_meter_longitude(py), computed on first need */
     while (sp > 0) {
         const int top = sp - 1;
         const uint8_t i = st_next[top];
@@ -48,10 +71,20 @@ __device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const do
         st_next[top] = i + 1;
         const uint32_t ch = nodes[st_node[top]].child[i];
         const DNode n = nodes[ch];
-        const double2 lo = low[ch];
-        if (box_le_fast(lo.x, lo.y, n.high_x, n.high_y, px, py, Lp, iLf, fb, ex)) {
+        int in = fx_box_screen(ibox[ch], w.X, w.Y, w.sc, f.cy);
+        double2 lo;
+        bool have_lo = false;
+        if (in < 0) {
+            lo = low[ch];
+            have_lo = true;
+            if (Lp == 0.0) Lp = dpm_lon_fast(w.py);
+            in = box_le_exact(lo.x, lo.y, kdbl(n.khx), kdbl(n.khy), w.px, w.py, Lp, ex) ? 1 : 0;
+        }
+        if (in) {
             if (n.type == kLeaf) {
-                if (py < lo.y || (py < n.high_y && px < lo.x)) {
+                if (!have_lo) lo = low[ch];
+                const uint64_t kly = dkey(lo.y), klx = dkey(lo.x);
+                if (w.ky < kly || (w.ky < n.khy && w.kx < klx)) {
                     emit(n.gid, kept);
                     ++kept;
                 }
@@ -67,41 +100,49 @@ __device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const do
     return kept;
 }
 
-__global__ void __launch_bounds__(128) k_filter_walk(const uint32_t *__restrict__ sorted, uint32_t N,
-                                                     const double2 *__restrict__ pts, const double *__restrict__ L,
-                                                     const uint32_t *__restrict__ obj_lv,
-                                                     const uint32_t *__restrict__ obj_leaf,
-                                                     const DNode *__restrict__ nodes, const double2 *__restrict__ low,
-                                                     uint32_t *__restrict__ qcount, uint32_t *__restrict__ qtmp,
-                                                     FastBox fb, ExactCtx ex, DevCounters *cnt) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-        const uint32_t pid = sorted[i];
-        const uint32_t lv = obj_lv[pid];
+struct FilterArgs {
+    const uint32_t *sorted;
+    const uint32_t *rank_of;
+    const double2 *sxy;
+    const longlong2 *sipos;
+    const float *sc;
+    const uint32_t *obj_lv;
+    const uint32_t *obj_leaf;
+    const DNode *nodes;
+    const double2 *low;
+    const longlong4 *ibox;
+    uint32_t N;
+    Frame f;
+    ExactCtx ex;
+    DevCounters *cnt;
+};
+
+__global__ void __launch_bounds__(128) k_filter_walk(FilterArgs a, uint32_t *__restrict__ qcount,
+                                                     uint32_t *__restrict__ qtmp) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
+        const uint32_t pid = a.sorted[i];
+        const uint32_t lv = a.obj_lv[pid];
         uint32_t kept = 0;
-        if (lv != obj_leaf[pid]) {
-            const double2 p = pts[pid];
+        if (lv != a.obj_leaf[pid]) {
+            const WalkPoint w = walk_point(a.sxy[i], a.sipos[i], a.sc[i], a.f);
             uint32_t *row = qtmp + (size_t)pid * kQInline;
-            kept = lookup_walk(nodes, low, lv, p.x, p.y, L[pid], fb, ex, cnt, [&](uint32_t gid, uint32_t k) {
+            kept = lookup_walk(a.nodes, a.low, a.ibox, lv, w, a.f, a.ex, a.cnt, [&](uint32_t gid, uint32_t k) {
                 if (k < kQInline) row[k] = gid;
             });
-            atomicAdd(&cnt->border_objects, 1u);
+            atomicAdd(&a.cnt->border_objects, 1u);
         }
         qcount[pid] = kept;
     }
 }
 
-__global__ void __launch_bounds__(128) k_filter_emit(uint32_t N, const double2 *__restrict__ pts,
-                                                     const double *__restrict__ L, const uint32_t *__restrict__ obj_lv,
-                                                     const DNode *__restrict__ nodes, const double2 *__restrict__ low,
-                                                     const uint32_t *__restrict__ qstart,
+__global__ void __launch_bounds__(128) k_filter_emit(FilterArgs a, const uint32_t *__restrict__ qstart,
                                                      const uint32_t *__restrict__ qtmp, uint32_t *__restrict__ qlist,
-                                                     uint32_t *__restrict__ tcount, uint64_t check_cap, FastBox fb, ExactCtx ex,
-                                                     DevCounters *cnt) {
-    for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < N; pid += gridDim.x * blockDim.x) {
+                                                     uint32_t *__restrict__ tcount, uint64_t check_cap) {
+    for (uint32_t pid = blockIdx.x * blockDim.x + threadIdx.x; pid < a.N; pid += gridDim.x * blockDim.x) {
         const uint32_t b = qstart[pid], e = qstart[pid + 1];
         if (b == e) continue;
         if ((uint64_t)e > check_cap) {
-            atomicOr(&cnt->error_flags, GLINT_EF_CHECKS_OVERFLOW);
+            atomicOr(&a.cnt->error_flags, GLINT_EF_CHECKS_OVERFLOW);
             continue;
         }
         const uint32_t n = e - b;
@@ -112,8 +153,9 @@ __global__ void __launch_bounds__(128) k_filter_emit(uint32_t N, const double2 *
             atomicAdd(&tcount[g], 1u);
         }
         if (n > (uint32_t)kQInline) {
-            const double2 p = pts[pid];
-            lookup_walk(nodes, low, obj_lv[pid], p.x, p.y, L[pid], fb, ex, cnt, [&](uint32_t gid, uint32_t k) {
+            const uint32_t r = a.rank_of[pid];
+            const WalkPoint w = walk_point(a.sxy[r], a.sipos[r], a.sc[r], a.f);
+            lookup_walk(a.nodes, a.low, a.ibox, a.obj_lv[pid], w, a.f, a.ex, a.cnt, [&](uint32_t gid, uint32_t k) {
                 if (k >= (uint32_t)kQInline && k < n) {
                     qlist[b + k] = gid;
                     atomicAdd(&tcount[gid], 1u);
@@ -143,21 +185,27 @@ __global__ void __launch_bounds__(256) k_filter_group(uint32_t N, const uint32_t
 cudaError_t launch_filter(glint_ctx *c) {
     cudaStream_t s = c->stream;
     const uint32_t N = c->N, G = c->G;
-    ExactCtx ex = make_exact(c);
-    FastBox fb;
-    const double r2 = c->cfg.reach_distance * c->cfg.reach_distance;
-    fb.iMf = (float)(1.0 / c->dpm_lat);
-    fb.r2lo = (float)(r2 * (1.0 - std::ldexp(1.0, -16)));
-    fb.r2hi = (float)(r2 * (1.0 + std::ldexp(1.0, -16)));
-    k_filter_walk<<<grid_for(N, 128, 152u * 16u), 128, 0, s>>>(c->d_sorted, N, c->d_pts, c->d_L, c->d_obj_lv,
-                                                                 c->d_obj_leaf, c->d_nodes, c->d_low, c->d_qcount,
-                                                                 c->d_qtmp, fb, ex, c->d_cnt);
+    FilterArgs a;
+    a.sorted = c->d_sorted;
+    a.rank_of = c->d_rank_of;
+    a.sxy = c->d_sxy;
+    a.sipos = c->d_sipos;
+    a.sc = c->d_sc;
+    a.obj_lv = c->d_obj_lv;
+    a.obj_leaf = c->d_obj_leaf;
+    a.nodes = c->d_nodes;
+    a.low = c->d_low;
+    a.ibox = c->d_ibox;
+    a.N = N;
+    a.f = c->frame;
+    a.ex = make_exact(c);
+    a.cnt = c->d_cnt;
+    k_filter_walk<<<grid_for(N, 128, 152u * 16u), 128, 0, s>>>(a, c->d_qcount, c->d_qtmp);
     scan_u32(c->d_qcount, c->d_qstart, N, c->d_scan_tmp, s);
     cudaMemsetAsync(c->d_tcount, 0, sizeof(uint32_t) * (G + 1), s);
     cudaMemsetAsync(c->d_tcursor, 0, sizeof(uint32_t) * G, s);
-    k_filter_emit<<<grid_for(N, 128, 152u * 16u), 128, 0, s>>>(N, c->d_pts, c->d_L, c->d_obj_lv, c->d_nodes, c->d_low,
-                                                                 c->d_qstart, c->d_qtmp,
-                                                                 c->d_qlist, c->d_tcount, c->check_cap, fb, ex, c->d_cnt);
+    k_filter_emit<<<grid_for(N, 128, 152u * 16u), 128, 0, s>>>(a, c->d_qstart, c->d_qtmp, c->d_qlist, c->d_tcount,
+                                                                 c->check_cap);
     scan_u32(c->d_tcount, c->d_tstart, G, c->d_scan_tmp, s);
     k_filter_group<<<grid_for(N, 256, 152u * 8u), 256, 0, s>>>(N, c->d_qstart, c->d_qlist, c->d_tstart, c->d_tcursor,
                                                                 c->d_tlist, c->check_cap);

@@ -28,7 +28,7 @@ constexpr uint8_t kStampEmit = 4;
 __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict__ stamp, TRec *__restrict__ tab,
                                                              uint64_t B, uint8_t st_now, uint32_t cur_time,
                                                              uint32_t min_plus1, uint32_t *__restrict__ tile_cnt,
-                                                             const double2 *__restrict__ pts, uint32_t N,
+                                                             const float2 *__restrict__ fpos, uint32_t N,
                                                              DevCounters *cnt) {
     __shared__ uint32_t red[3][kIdThreads / 32];
     const uint64_t base = (uint64_t)blockIdx.x * kIdTile + (uint64_t)threadIdx.x * kIdItems;
@@ -58,8 +58,8 @@ __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict
                 nr.w0 = pw;
                 nr.w1 = cur_time;
                 if (pa < N && pb < N) {
-                    const double2 A = pts[pa], Bp = pts[pb];
-                    const float ax = (float)A.x, ay = (float)A.y, bx = (float)Bp.x, by = (float)Bp.y;
+                    const float2 A = fpos[pa], Bp = fpos[pb];
+                    const float ax = A.x, ay = A.y, bx = Bp.x, by = Bp.y;
                     nr.mbr[0] = min(fenc(ax), fenc(bx));
                     nr.mbr[1] = min(fenc(ay), fenc(by));
                     nr.mbr[2] = max(fenc(ax), fenc(bx));
@@ -189,7 +189,7 @@ cudaError_t launch_identify(glint_ctx *c, uint32_t cur_time) {
     const uint8_t st_now = stamp_of(c->step_index);
     const uint32_t min_plus1 = c->cfg.min_meet_time + 1;
     k_expire_count<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, st_now, cur_time, min_plus1,
-                                                          c->d_tile_cnt, c->d_pts, c->N, c->d_cnt);
+                                                          c->d_tile_cnt, c->d_fpos, c->N, c->d_cnt);
     scan_u32(c->d_tile_cnt, c->d_tile_off, tiles, c->d_scan_tmp, s);
     k_expire_emit<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, cur_time, c->d_tile_cnt,
                                                          c->d_tile_off, c->d_log, c->log_cap, c->d_cnt);

@@ -26,16 +26,19 @@ __global__ void __launch_bounds__(256) k_descend(const double2 *__restrict__ pts
                                                  uint32_t N, const DNode *__restrict__ nodes, uint32_t S, uint32_t G,
                                                  double xb, double yb,
                                                  uint32_t *__restrict__ obj_gid, uint32_t *__restrict__ obj_lv,
-                                                 uint32_t *__restrict__ obj_leaf, double *__restrict__ objL,
-                                                 uint32_t *__restrict__ grid_count, DevCounters *cnt) {
+                                                 uint32_t *__restrict__ obj_leaf, uint32_t *__restrict__ grid_count,
+                                                 DevCounters *cnt) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
         const uint32_t pid = order[i];
         const double2 p = pts[pid];
+        /* the comparisons of filter.cpp:231,235-236 on order-preserving keys */
+        const uint64_t kx = dkey(p.x), ky = dkey(p.y);
+        const uint64_t kxb = dkey(__dadd_rn(p.x, xb)), kyb = dkey(__dadd_rn(p.y, yb));
         uint32_t cur = 0, lv = 0, gid = 0;
         DNode n = nodes[0];
         int depth = 0;
         for (;;) {
-            const int child = (p.y > n.mid_y) * 2 + (p.x > n.mid_x);
+            const int child = (ky > n.kmy) * 2 + (kx > n.kmx);
             cur = n.child[child];
             if (cur >= S || ++depth >= kMaxDepth) {
                 /* a corrupt or too deep schema: keep memory safe and report */
@@ -44,7 +47,7 @@ __global__ void __launch_bounds__(256) k_descend(const double2 *__restrict__ pts
                 break;
             }
             n = nodes[cur];
-            if (__dadd_rn(p.x, xb) < n.high_x && __dadd_rn(p.y, yb) < n.high_y) lv = cur;
+            if (kxb < n.khx && kyb < n.khy) lv = cur;
             if (n.type == kLeaf) {
                 gid = n.gid < G ? n.gid : 0u;
                 break;
@@ -58,7 +61,6 @@ __global__ void __launch_bounds__(256) k_descend(const double2 *__restrict__ pts
         obj_gid[pid] = gid;
         obj_lv[pid] = lv;
         obj_leaf[pid] = cur;
-        objL[pid] = dpm_lon_fast(p.y);
         atomicAdd(&grid_count[gid], 1u);
     }
 }
@@ -199,16 +201,35 @@ __global__ void __launch_bounds__(1024) k_segsort_block(const uint32_t *__restri
     }
 }
 
-/* coordinates and L in leaf-major order, and each object's sorted position */
+/* per object, in leaf-major order: the coordinates, their fixed-point and
+ * FP32 forms and the screening scale cx; L with CUDA sin for the plain form;
+ * each object's sorted position */
+struct GatherOut {
+    double2 *sxy;
+    longlong2 *sipos;
+    float2 *sfpos;
+    float *sc;
+    double *sL;        /* null: not needed */
+    float2 *fpos;      /* by object id */
+    uint32_t *rank_of;
+};
+
 __global__ void __launch_bounds__(256) k_gather(const uint32_t *__restrict__ sorted, uint32_t N,
-                                                const double2 *__restrict__ pts, const double *__restrict__ L,
-                                                double2 *__restrict__ sxy, double *__restrict__ sL,
-                                                uint32_t *__restrict__ rank_of) {
+                                                const double2 *__restrict__ pts, GatherOut o, Frame f) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < N; i += gridDim.x * blockDim.x) {
-        uint32_t pid = sorted[i];
-        sxy[i] = pts[pid];
-        sL[i] = L[pid];
-        rank_of[pid] = i;
+        const uint32_t pid = sorted[i];
+        const double2 p = pts[pid];
+        o.sxy[i] = p;
+        bool clamped = false;
+        const long long X = fx_coord(p.x, f.ox, f.S, &clamped);
+        const long long Y = fx_coord(p.y, f.oy, f.S, &clamped);
+        o.sipos[i] = make_longlong2(X, Y);
+        o.sc[i] = clamped ? __int_as_float(0x7fc00000) : c_of_lat(p.y, f);
+        const float2 fp = make_float2((float)p.x, (float)p.y);
+        o.sfpos[i] = fp;
+        o.fpos[pid] = fp;
+        if (o.sL) o.sL[i] = dpm_lon_fast(p.y);
+        o.rank_of[pid] = i;
     }
 }
 
@@ -219,7 +240,7 @@ cudaError_t launch_partition(glint_ctx *c, uint32_t /*cur_time*/) {
     cudaMemsetAsync(c->d_grid_cursor, 0, sizeof(uint32_t) * G, s);
     k_descend<<<grid_for(N, 256, 152u * 8u), 256, 0, s>>>(c->d_pts, c->d_order, N, c->d_nodes, c->S, G, c->x_buffer,
                                                            c->y_buffer, c->d_obj_gid, c->d_obj_lv, c->d_obj_leaf,
-                                                           c->d_L, c->d_grid_count, c->d_cnt);
+                                                           c->d_grid_count, c->d_cnt);
     scan_u32(c->d_grid_count, c->d_grid_start, G, c->d_scan_tmp, s);
     k_scatter<<<grid_for(N, 256, 152u * 8u), 256, 0, s>>>(c->d_obj_gid, N, c->d_grid_start, c->d_grid_cursor,
                                                            c->d_sorted);
@@ -229,8 +250,15 @@ cudaError_t launch_partition(glint_ctx *c, uint32_t /*cur_time*/) {
                                                        c->d_cnt);
     k_segsort_block<<<152, 1024, kBlockSortMax * sizeof(uint32_t), s>>>(c->d_big, c->d_grid_start, c->d_grid_count,
                                                                         c->d_sorted, c->d_cnt);
-    k_gather<<<grid_for(N, 256, 152u * 8u), 256, 0, s>>>(c->d_sorted, N, c->d_pts, c->d_L, c->d_sxy, c->d_sL,
-                                                          c->d_rank_of);
+    GatherOut o;
+    o.sxy = c->d_sxy;
+    o.sipos = c->d_sipos;
+    o.sfpos = c->d_sfpos;
+    o.sc = c->d_sc;
+    o.sL = c->cfg.precision_mode == 1 ? nullptr : c->d_sL;
+    o.fpos = c->d_fpos;
+    o.rank_of = c->d_rank_of;
+    k_gather<<<grid_for(N, 256, 152u * 8u), 256, 0, s>>>(c->d_sorted, N, c->d_pts, o, c->frame);
     return cudaGetLastError();
 }
 

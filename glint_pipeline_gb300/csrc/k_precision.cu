@@ -1,22 +1,16 @@
 /*
- * k_precision.cu -- the precision form of the refine stage: candidate pairs
- * are first tested in FP32 on coordinates relative to the leaf, and only the
- * pairs whose FP32 distance lies inside a guard band around the reach are
- * re-tested with the reference's exact FP64 arithmetic (point_le_exact), so
- * the contact set - and every meeting - stays identical to the reference's.
+ * k_precision.cu -- the precision form of the refine stage: every candidate
+ * pair is first screened in FP32 on exact fixed-point coordinate differences
+ * (the Frame of glint_device.cuh), and only the pairs whose screened squared
+ * distance lies inside the guard band around r^2 are re-tested with the
+ * reference's FP64 arithmetic (point_le_exact), so the contact set - and every
+ * meeting - stays identical to the reference's.
  *
- * Guard band.  For a tile with origin o (its first member), each object keeps
- * u = fl32(x - o.x), v = fl32(y - o.y) (degrees; the FP64 subtraction is exact
- * for nearby longitudes) and iL = fl32(1/L(y)).  For a pair with p1 = i the
- * reference decides sqrt(X^2 + Y^2) <= r with X = (x_i - x_j)/L_i and
- * Y = (y_i - y_j)/dpm_lat (geometry/geometry.h:40-48).  With unit roundoff
- * u = 2^-24 the FP32 values fx = (u_i - u_j) iL_i, fy = (v_i - v_j) iM obey
- *   |fx - X| <= u (3|X| + 2 (|u_i| + |u_j|) iL_i),   likewise for fy,
- * and near the threshold (|X|, |Y| <= r) the FP32 square q = fx^2 + fy^2 obeys
- *   |q - (X^2 + Y^2)| <= u (16 r^2 + 4 r W)
- * where W = (|u_i| + |u_j|) iL_i + (|v_i| + |v_j|) iM is the pair's offset
- * size in metres.  The band is twice that; outside it the FP32 decision equals
- * the reference's (the FP64 rounding of the reference is ~2^-50 relative).
+ * The reference's test (tracing/refinement.cpp:19-31 with Point::distance,
+ * geometry/geometry.h:40-48) divides the longitude difference by L(y1) of the
+ * checking object; the screen multiplies the integer difference by that
+ * object's cx = 1/(L(y1) S).  No FP64 instruction runs per pair outside the
+ * band: on sm_103a FP64 issues at a small fraction of the FP32 rate.
  */
 #include "refine_common.cuh"
 
@@ -24,37 +18,28 @@ namespace glint {
 
 constexpr int kPrecWarps = 4;
 
-struct PrecParams {
-    float r2;        /* r^2 */
-    float iMf;       /* 1 / dpm_lat */
-    float band_k0;   /* 2 * 2^-24 * 16 r^2 */
-    float band_k1;   /* 2 * 2^-24 * 4 r */
-};
-
-__device__ inline int prec_test(float du, float dv, float iL, float w_m, const PrecParams &pp) {
-    const float fx = du * iL, fy = dv * pp.iMf;
-    const float q = fx * fx + fy * fy;
-    const float band = pp.band_k0 + pp.band_k1 * w_m;
-    if (q < pp.r2 - band) return 1;
-    if (q > pp.r2 + band) return 0;
-    return -1; /* inside the guard band: decide exactly */
+/* one screened test; p1 scale cx, p2 scale c2 (a NaN in either forces the
+ * exact path) */
+__device__ inline int screen_pair(long long dx, long long dy, float cx, float c2, const Frame &f) {
+    const Screen s = make_screen(__fmaf_rn(0.0f, c2, cx), f);
+    return fx_screen(dx, dy, s, f.cy);
 }
 
-__global__ void __launch_bounds__(32 * kPrecWarps) k_refine_fp32(RefineArgs a, PrecParams pp) {
+__global__ void __launch_bounds__(32 * kPrecWarps) k_refine_fp32(RefineArgs a) {
     extern __shared__ unsigned char smem_raw[];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const uint32_t cap = a.cap;
-    /* per warp: x y L (double), u v iL (float), id (u32), queue */
-    const size_t per_warp = (size_t)cap * 40 + sizeof(QEntry) * kQueue + 64;
+    /* per warp: X Y (i64), cx fx fy (f32), id (u32), queue */
+    const size_t per_warp = (size_t)cap * 32 + sizeof(QEntry) * kQueue + 64;
     unsigned char *base = smem_raw + (size_t)w * ((per_warp + 63) & ~(size_t)63);
-    double *sx = reinterpret_cast<double *>(base);
-    double *sy = sx + cap;
-    double *sLm = sy + cap;
-    float *su = reinterpret_cast<float *>(sLm + cap);
-    float *sv = su + cap;
-    float *siL = sv + cap;
-    uint32_t *sid = reinterpret_cast<uint32_t *>(siL + cap);
+    long long *sX = reinterpret_cast<long long *>(base);
+    long long *sY = sX + cap;
+    float *sC = reinterpret_cast<float *>(sY + cap);
+    float *sFx = sC + cap;
+    float *sFy = sFx + cap;
+    uint32_t *sid = reinterpret_cast<uint32_t *>(sFy + cap);
     QEntry *Q = reinterpret_cast<QEntry *>(((uintptr_t)(sid + cap) + 15) & ~(uintptr_t)15);
+    const Frame f = a.f;
 
     unsigned long long cand = 0, hits = 0;
     uint32_t band = 0;
@@ -69,95 +54,88 @@ __global__ void __launch_bounds__(32 * kPrecWarps) k_refine_fp32(RefineArgs a, P
         const uint32_t s0 = a.grid_start[g];
         const uint32_t cnt_g = a.grid_count[g];
         const uint32_t k = cnt_g < cap ? cnt_g : cap;
-        const double2 org = a.sxy[s0];
         for (uint32_t i = lane; i < k; i += 32) {
-            const double2 p = a.sxy[s0 + i];
-            const double L = a.sL[s0 + i];
-            sx[i] = p.x;
-            sy[i] = p.y;
-            sLm[i] = L;
-            su[i] = (float)(p.x - org.x);
-            sv[i] = (float)(p.y - org.y);
-            siL[i] = (float)(1.0 / L);
+            const longlong2 ip = a.sipos[s0 + i];
+            const float2 fp = a.sfpos[s0 + i];
+            sX[i] = ip.x;
+            sY[i] = ip.y;
+            sC[i] = a.sc[s0 + i];
+            sFx[i] = fp.x;
+            sFy[i] = fp.y;
             sid[i] = a.sorted[s0 + i];
         }
         __syncwarp();
+        /* inside checks: p1 = member i, p2 = member j > i */
         for (uint32_t i = 0; i + 1 < k; ++i) {
-            const float ui = su[i], vi = sv[i], iLi = siL[i];
-            const float aui = fabsf(ui), avi = fabsf(vi);
+            const long long Xi = sX[i], Yi = sY[i];
+            const float ci = sC[i];
             const uint32_t p1 = sid[i];
             for (uint32_t jb = i + 1; jb < k; jb += 32) {
                 const uint32_t j = jb + lane;
                 bool hit = false;
                 unsigned long long pw = 0;
-                float fx1 = 0.f, fy1 = 0.f, fx2 = 0.f, fy2 = 0.f;
                 if (j < k) {
                     ++cand;
-                    const float uj = su[j], vj = sv[j];
-                    const float wm = (aui + fabsf(uj)) * iLi + (avi + fabsf(vj)) * pp.iMf;
-                    int r = prec_test(ui - uj, vi - vj, iLi, wm, pp);
+                    int r = screen_pair(Xi - sX[j], Yi - sY[j], ci, sC[j], f);
                     if (r < 0) {
                         ++band;
-                        r = point_le_exact(sx[i], sy[i], sx[j], sy[j], sLm[i], a.ex) ? 1 : 0;
+                        const double2 P = a.sxy[s0 + i], Q2 = a.sxy[s0 + j];
+                        r = point_le_exact(P.x, P.y, Q2.x, Q2.y, dpm_lon_fast(P.y), a.ex) ? 1 : 0;
                     }
                     hit = r == 1;
                     if (hit) {
                         ++hits;
                         pw = pair_word(p1, sid[j]);
-                        fx1 = (float)sx[i];
-                        fy1 = (float)sy[i];
-                        fx2 = (float)sx[j];
-                        fy2 = (float)sy[j];
                     }
                 }
-                enqueue(a, Q, qn, hit, pw, prio_pack(0, p1, 0, j), fx1, fy1, fx2, fy2);
+                enqueue(a, Q, qn, hit, pw, prio_pack(0, p1, 0, j), sFx[i], sFy[i], hit ? sFx[j] : 0.f,
+                        hit ? sFy[j] : 0.f);
             }
         }
+        /* cross-leaf checks that target this leaf: p1 = the querier */
         const uint32_t tb = a.tstart[g], te = a.tstart[g + 1];
         for (uint32_t t = tb; t < te; ++t) {
             const uint2 qe = a.tlist[t];
             const uint32_t q = qe.x;
-            const double2 qp = a.pts[q];
-            const double Lq = a.L[q];
+            const uint32_t qr = a.rank_of[q];
+            const longlong2 qi = a.sipos[qr];
+            const float cq = a.sc[qr];
+            const float2 qf = a.sfpos[qr];
             const uint32_t qgid = a.obj_gid[q];
-            const bool qstored = (a.rank_of[q] - a.grid_start[qgid]) < cap;
-            const float uq = (float)(qp.x - org.x), vq = (float)(qp.y - org.y), iLq = (float)(1.0 / Lq);
-            const float auq = fabsf(uq), avq = fabsf(vq);
+            const bool qstored = (qr - a.grid_start[qgid]) < cap;
             for (uint32_t jb = 0; jb < k; jb += 32) {
                 const uint32_t j = jb + lane;
                 bool hit = false;
                 unsigned long long pw = 0;
-                float fx2 = 0.f, fy2 = 0.f;
                 if (j < k) {
                     ++cand;
-                    const float uj = su[j], vj = sv[j];
-                    const float auj = fabsf(uj), avj = fabsf(vj);
-                    int r = prec_test(uq - uj, vq - vj, iLq, (auq + auj) * iLq + (avq + avj) * pp.iMf, pp);
+                    const long long dx = qi.x - sX[j], dy = qi.y - sY[j];
+                    int r = screen_pair(dx, dy, cq, sC[j], f);
                     if (r < 0) {
                         ++band;
-                        r = point_le_exact(qp.x, qp.y, sx[j], sy[j], Lq, a.ex) ? 1 : 0;
+                        const double2 P = a.sxy[qr], M = a.sxy[s0 + j];
+                        r = point_le_exact(P.x, P.y, M.x, M.y, dpm_lon_fast(P.y), a.ex) ? 1 : 0;
                     }
                     hit = r == 1;
                     if (hit) {
                         ++hits;
                         const uint32_t m = sid[j];
+                        /* the same pair tested from m's side comes first in the
+                         * reference's order when m < q; keep only one event */
                         if (q > m && qstored && has_check(a, m, qgid)) {
-                            /* the mirrored test, p1 = m */
-                            int r2 = prec_test(uj - uq, vj - vq, siL[j], (auq + auj) * siL[j] + (avq + avj) * pp.iMf, pp);
+                            int r2 = screen_pair(dx, dy, sC[j], cq, f);
                             if (r2 < 0) {
                                 ++band;
-                                r2 = point_le_exact(sx[j], sy[j], qp.x, qp.y, sLm[j], a.ex) ? 1 : 0;
+                                const double2 P = a.sxy[qr], M = a.sxy[s0 + j];
+                                r2 = point_le_exact(M.x, M.y, P.x, P.y, dpm_lon_fast(M.y), a.ex) ? 1 : 0;
                             }
                             if (r2 == 1) hit = false;
                         }
-                        if (hit) {
-                            pw = pw_of(q, m);
-                            fx2 = (float)sx[j];
-                            fy2 = (float)sy[j];
-                        }
+                        if (hit) pw = pw_of(q, m);
                     }
                 }
-                enqueue(a, Q, qn, hit, pw, prio_pack(1, q, qe.y, j), (float)qp.x, (float)qp.y, fx2, fy2);
+                enqueue(a, Q, qn, hit, pw, prio_pack(1, q, qe.y, j), qf.x, qf.y, hit ? sFx[j] : 0.f,
+                        hit ? sFy[j] : 0.f);
             }
         }
         __syncwarp();
@@ -176,19 +154,12 @@ __global__ void __launch_bounds__(32 * kPrecWarps) k_refine_fp32(RefineArgs a, P
 }
 
 size_t refine_prec_smem_bytes(uint32_t cap) {
-    const size_t per_warp = (size_t)cap * 40 + sizeof(QEntry) * kQueue + 64;
+    const size_t per_warp = (size_t)cap * 32 + sizeof(QEntry) * kQueue + 64;
     return (size_t)kPrecWarps * ((per_warp + 63) & ~(size_t)63);
 }
 
 cudaError_t launch_refine_precision(glint_ctx *c, const RefineArgs &a) {
-    PrecParams pp;
-    const double r = c->cfg.reach_distance;
-    pp.r2 = (float)(r * r);
-    pp.iMf = (float)(1.0 / c->dpm_lat);
-    const double u = std::ldexp(1.0, -24);
-    pp.band_k0 = (float)(2.0 * u * 16.0 * r * r);
-    pp.band_k1 = (float)(2.0 * u * 4.0 * r);
-    k_refine_fp32<<<152 * 8, 32 * kPrecWarps, refine_prec_smem_bytes(c->cap), c->stream>>>(a, pp);
+    k_refine_fp32<<<152 * 8, 32 * kPrecWarps, refine_prec_smem_bytes(c->cap), c->stream>>>(a);
     return cudaGetLastError();
 }
 

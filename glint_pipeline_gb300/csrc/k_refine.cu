@@ -91,10 +91,11 @@ __global__ void __launch_bounds__(32 * kRefineWarps) k_refine_fp64(RefineArgs a)
         for (uint32_t t = tb; t < te; ++t) {
             const uint2 qe = a.tlist[t];
             const uint32_t q = qe.x;
-            const double2 qp = a.pts[q];
-            const double Lq = a.L[q];
+            const uint32_t qr = a.rank_of[q];
+            const double2 qp = a.sxy[qr];
+            const double Lq = a.sL[qr];
             const uint32_t qgid = a.obj_gid[q];
-            const bool qstored = (a.rank_of[q] - a.grid_start[qgid]) < cap;
+            const bool qstored = (qr - a.grid_start[qgid]) < cap;
             const float fqx = (float)qp.x, fqy = (float)qp.y;
             for (uint32_t jb = 0; jb < k; jb += 32) {
                 const uint32_t j = jb + lane;
@@ -150,13 +151,14 @@ RefineArgs refine_args(glint_ctx *c) {
     a.sL = c->d_sL;
     a.tstart = c->d_tstart;
     a.tlist = c->d_tlist;
-    a.pts = c->d_pts;
-    a.L = c->d_L;
+    a.sipos = c->d_sipos;
+    a.sfpos = c->d_sfpos;
+    a.sc = c->d_sc;
+    a.f = c->frame;
     a.obj_gid = c->d_obj_gid;
     a.rank_of = c->d_rank_of;
     a.qstart = c->d_qstart;
     a.qlist = c->d_qlist;
-    a.leaf_low = nullptr;
     a.tab = c->d_tab;
     a.stamp = c->d_stamp;
     a.newlist = c->d_new;
@@ -202,8 +204,8 @@ __device__ inline ulonglong2 cas128(TRec *r, ulonglong2 expect, ulonglong2 desir
     return make_ulonglong2((unsigned long long)o, (unsigned long long)(o >> 64));
 }
 
-__device__ inline void touch_box(TRec &r, const double2 &A, const double2 &Bp) {
-    const float ax = (float)A.x, ay = (float)A.y, bx = (float)Bp.x, by = (float)Bp.y;
+__device__ inline void touch_box(TRec &r, const float2 &A, const float2 &Bp) {
+    const float ax = A.x, ay = A.y, bx = Bp.x, by = Bp.y;
     uint4 m = *reinterpret_cast<const uint4 *>(r.mbr);
     m.x = min(m.x, min(fenc(ax), fenc(bx)));
     m.y = min(m.y, min(fenc(ay), fenc(by)));
@@ -214,7 +216,7 @@ __device__ inline void touch_box(TRec &r, const double2 &A, const double2 &Bp) {
 
 __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ list, TRec *tab, uint8_t *stamp,
                                                 uint64_t B, uint64_t Bm, uint64_t new_cap,
-                                                const double2 *__restrict__ pts, uint32_t N, uint8_t st,
+                                                const float2 *__restrict__ fpos, uint32_t N, uint8_t st,
                                                 DevCounters *cnt) {
     const unsigned long long n0 = cnt->new_keys;
     const unsigned long long n = n0 < new_cap ? n0 : new_cap;
@@ -248,7 +250,7 @@ __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ lis
                 if (seen.x == plain) {
                     /* the carried pair's own committed entry */
                     const uint32_t pa = pair_a(plain), pb = pair_b(plain);
-                    if (pa < N && pb < N) touch_box(tab[slot], pts[pa], pts[pb]);
+                    if (pa < N && pb < N) touch_box(tab[slot], fpos[pa], fpos[pb]);
                     stamp[slot] = st;
                     done = true;
                     break;
@@ -278,7 +280,7 @@ __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ lis
 cudaError_t launch_insert(glint_ctx *c, uint32_t cur_time) {
     const uint8_t st = stamp_of(c->step_index);
     (void)cur_time;
-    k_insert<<<152 * 8, 256, 0, c->stream>>>(c->d_new, c->d_tab, c->d_stamp, c->B, c->Bm, c->new_cap, c->d_pts, c->N,
+    k_insert<<<152 * 8, 256, 0, c->stream>>>(c->d_new, c->d_tab, c->d_stamp, c->B, c->Bm, c->new_cap, c->d_fpos, c->N,
                                              st, c->d_cnt);
     return cudaGetLastError();
 }

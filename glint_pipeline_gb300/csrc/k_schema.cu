@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) k_sch_collect(DNode *__restrict__ nodes, 
             bool cond = false;
             if (c > gc) {
                 const double2 lo = low[s];
-                cond = width_gt_exact(lo.x, n.high_x, lo.y, two_r, ex);
+                cond = width_gt_exact(lo.x, kdbl(n.khx), lo.y, two_r, ex);
             }
             int16_t of = 0;
             if (cond) {
@@ -353,6 +353,7 @@ __global__ void __launch_bounds__(256) k_sch_apply_merge(DNode *__restrict__ nod
 }
 
 __global__ void __launch_bounds__(256) k_sch_apply_split(DNode *__restrict__ nodes, double2 *__restrict__ low,
+                                                         longlong4 *__restrict__ ibox, Frame fr,
                                                          const uint8_t *__restrict__ flags,
                                                          const uint32_t *__restrict__ events, const uint4 *evdata,
                                                          uint32_t *__restrict__ grid_count, const DevCounters *cnt) {
@@ -368,8 +369,12 @@ __global__ void __launch_bounds__(256) k_sch_apply_split(DNode *__restrict__ nod
         grid_count[gs.w] = 0;
         const DNode pn = nodes[p];
         const double2 pl = low[p];
-        const double xhalf = __dsub_rn(pn.mid_x, pl.x);
-        const double yhalf = __dsub_rn(pn.mid_y, pl.y);
+        const double pmx = kdbl(pn.kmx), pmy = kdbl(pn.kmy);
+        /* split_node (tracing/filter.cpp:347-370): children are the parent's
+         * quadrants, offset by half the parent's extent; the boxes are also
+         * kept in fixed point for the filter's screening */
+        const double xhalf = __dsub_rn(pmx, pl.x);
+        const double yhalf = __dsub_rn(pmy, pl.y);
         const uint32_t ch[4] = {cs.x, cs.y, cs.z, cs.w};
         const uint32_t gg[4] = {gs.x, gs.y, gs.z, gs.w};
         for (int k = 0; k < 4; ++k) {
@@ -378,10 +383,13 @@ __global__ void __launch_bounds__(256) k_sch_apply_split(DNode *__restrict__ nod
             DNode c;
             const double lx = __dadd_rn(pl.x, ox);
             const double ly = __dadd_rn(pl.y, oy);
-            c.high_x = __dadd_rn(pn.mid_x, ox);
-            c.high_y = __dadd_rn(pn.mid_y, oy);
-            c.mid_x = __dmul_rn(__dadd_rn(lx, c.high_x), 0.5);
-            c.mid_y = __dmul_rn(__dadd_rn(ly, c.high_y), 0.5);
+            const double hx = __dadd_rn(pmx, ox);
+            const double hy = __dadd_rn(pmy, oy);
+            c.khx = dkey(hx);
+            c.khy = dkey(hy);
+            c.kmx = dkey(__dmul_rn(__dadd_rn(lx, hx), 0.5));
+            c.kmy = dkey(__dmul_rn(__dadd_rn(ly, hy), 0.5));
+            ibox[ch[k]] = fx_box(lx, ly, hx, hy, fr);
             c.child[0] = c.child[1] = c.child[2] = c.child[3] = 0;
             c.gid = gg[k];
             c.type = kLeaf;
@@ -425,7 +433,8 @@ cudaError_t launch_schema_update(glint_ctx *c) {
                                                                        c->d_evlevel, kWinCap, c->d_cnt);
     k_sch_apply_merge<<<152, 256, 0, s>>>(c->d_nodes, c->d_split, c->d_newgid, c->d_evlist, c->d_evdata,
                                           c->d_grid_count, c->d_cnt);
-    k_sch_apply_split<<<152, 256, 0, s>>>(c->d_nodes, c->d_low, c->d_split, c->d_evlist, c->d_evdata,
+    k_sch_apply_split<<<152, 256, 0, s>>>(c->d_nodes, c->d_low, c->d_ibox, c->frame, c->d_split, c->d_evlist,
+                                          c->d_evdata,
                                           c->d_grid_count, c->d_cnt);
     return cudaGetLastError();
 }

@@ -28,19 +28,20 @@ struct RefineArgs {
     const double *sL;
     const uint32_t *tstart;
     const uint2 *tlist;
-    const double2 *pts;
-    const double *L;
+    const longlong2 *sipos;    /* fixed-point coordinates, leaf-major */
+    const float2 *sfpos;       /* FP32 coordinates, leaf-major */
+    const float *sc;           /* screening scale cx, leaf-major */
     const uint32_t *obj_gid;
     const uint32_t *rank_of;
     const uint32_t *qstart;
     const uint32_t *qlist;
-    const double2 *leaf_low;   /* per grid id: low corner of the leaf (precision form) */
     TRec *tab;
     uint8_t *stamp;
     NewEntry *newlist;
     uint64_t B, Bm, new_cap;
     uint32_t cap;
     uint8_t st;
+    Frame f;
     ExactCtx ex;
     DevCounters *cnt;
 };
