@@ -20,11 +20,11 @@ import os
 import numpy as np
 
 from . import _abi
-from ._abi import GlintConfig, GlintStepStats, MEETING_DTYPE, SCHEMA_DTYPE, GlintError
+from ._abi import GlintConfig, GlintStepStats, MEETING_DTYPE, SCHEMA_DTYPE, SEARCH_DTYPE, GlintError
 
 __all__ = [
     "Configuration", "DeviceBench", "cuda_create_device_bench", "process_with_gpu", "GlintError",
-    "MEETING_DTYPE", "SCHEMA_DTYPE", "library_path", "load_library",
+    "MEETING_DTYPE", "SCHEMA_DTYPE", "SEARCH_DTYPE", "library_path", "load_library",
 ]
 
 library_path = _abi.library_path
@@ -140,6 +140,25 @@ class DeviceBench:
             if st != 0:
                 raise GlintError(st, self.last_error())
         return out
+
+    def active_search(self, pids, cap: int | None = None) -> np.ndarray:
+        """Active meetings of the listed objects after the last step
+        (search_multi, cuda/geometry.cu:605-663), in bucket order."""
+        p = np.ascontiguousarray(pids, dtype=np.uint32)
+        n = ctypes.c_uint64()
+        if cap is None:
+            st = self.lib.glint_active_search(self.h, p.ctypes.data_as(ctypes.c_void_p), p.shape[0], None, 0,
+                                              ctypes.byref(n))
+            if st != 0:
+                raise GlintError(st, self.last_error())
+            cap = n.value
+        out = np.zeros(int(cap), dtype=SEARCH_DTYPE)
+        st = self.lib.glint_active_search(self.h, p.ctypes.data_as(ctypes.c_void_p), p.shape[0],
+                                          out.ctypes.data_as(ctypes.c_void_p) if cap else None, int(cap),
+                                          ctypes.byref(n))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        return out[: min(int(n.value), int(cap))]
 
     # -- state ------------------------------------------------------------------
     def schema(self):

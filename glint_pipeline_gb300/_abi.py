@@ -108,6 +108,9 @@ SCHEMA_DTYPE = np.dtype([
     ("low", "<f8", (2,)), ("high", "<f8", (2,)), ("children", "<u4", (4,)),
 ])
 assert SCHEMA_DTYPE.itemsize == 80 and MEETING_DTYPE.itemsize == 32
+# glint_search_info = search_info_unit (tracing/workbench.h:85-88)
+SEARCH_DTYPE = np.dtype([("pid", "<u4"), ("target", "<u4"), ("start", "<u4"), ("end", "<u4"), ("mbr", "<f4", (4,))])
+assert SEARCH_DTYPE.itemsize == 32
 
 
 def load_library(path: str | None = None):
@@ -137,6 +140,7 @@ def load_library(path: str | None = None):
     lib.glint_get_capacities.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32), ctypes.POINTER(u64)]
     lib.glint_stream.restype = vp
     lib.glint_stream.argtypes = [vp]
+    lib.glint_active_search.argtypes = [vp, vp, u32, vp, u64, ctypes.POINTER(u64)]
     lib.glint_gen_create.argtypes = [vp, u32, vp, u32, u32, u32, ctypes.POINTER(vp)]
     lib.glint_gen_step.argtypes = [vp, vp, vp]
     lib.glint_gen_destroy.argtypes = [vp]

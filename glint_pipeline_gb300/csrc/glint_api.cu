@@ -174,7 +174,7 @@ void free_all(glint_ctx *c) {
                     c->d_events, c->d_evpos, c->d_evlist, c->d_evdata, c->d_evlevel, c->d_big, c->d_qcount,
                     c->d_qstart, c->d_qlist, c->d_qtmp, c->d_tcount, c->d_tstart, c->d_tcursor, c->d_tlist, c->d_tab,
                     c->d_stamp, c->d_new, c->d_tile_cnt, c->d_tile_off, c->d_log, c->d_cnt, c->d_coef,
-                    c->d_scan_tmp};
+                    c->d_scan_tmp, c->d_qbits, c->d_qpids, c->d_qout, c->d_qn};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     if (c->h_cnt) cudaFreeHost(c->h_cnt);

@@ -343,9 +343,21 @@ __device__ inline Screen make_screen(float cx, const Frame &f) {
     return s;
 }
 
+/* integer -> FP32 on the FP32 pipe (I2F issues on the narrow FP64 pipe of
+ * sm_103a): for |v| < 2^22 the bits 0x4B400000 + v are the float
+ * 1.5*2^23 + v exactly, so one subtraction recovers v */
+__device__ inline float small_to_f(int v) { return __fsub_rn(__int_as_float(0x4B400000 + v), 12582912.0f); }
+
+/* correctly rounded FP32 value of d */
 __device__ inline float fx_to_f(long long d) {
-    const long long lim = 1ll << 31;
-    return (d > -lim && d < lim) ? (float)(int)d : __ll2float_rn(d);
+    const long long s = 1ll << 22, w = 1ll << 44;
+    if (d > -s && d < s) return small_to_f((int)d);
+    if (d > -w && d < w) {
+        /* d = hi 2^22 + lo with lo in [0, 2^22): one rounding in the fma */
+        const int hi = (int)(d >> 22), lo = (int)(d & 0x3FFFFF);
+        return __fmaf_rn(small_to_f(hi), 4194304.0f, small_to_f(lo));
+    }
+    return __ll2float_rn(d);
 }
 
 /* 1 within reach, 0 beyond, -1 inside the guard band (or a NaN scale);

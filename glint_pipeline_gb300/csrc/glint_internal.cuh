@@ -145,6 +145,13 @@ struct glint_ctx {
     /* output */
     glint_meeting *d_log = nullptr;
 
+    /* active search scratch, allocated on first use */
+    uint32_t *d_qbits = nullptr;
+    uint32_t *d_qpids = nullptr;
+    glint_search_info *d_qout = nullptr;
+    unsigned long long *d_qn = nullptr;
+    uint64_t qbits_cap = 0, qpids_cap = 0, qout_cap = 0;
+
     /* misc */
     glint::DevCounters *d_cnt = nullptr;
     glint::DevCounters *h_cnt = nullptr;   /* pinned */

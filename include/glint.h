@@ -200,6 +200,30 @@ glint_status glint_get_capacities(const glint_ctx *ctx, uint32_t *schema_capacit
 /* the context's cudaStream_t */
 void *glint_stream(glint_ctx *ctx);
 
+/* ---- active contact search --------------------------------------------
+ * search_info_unit (tracing/workbench.h:85-88): one active meeting of a
+ * listed object. */
+typedef struct glint_search_info {
+    uint32_t pid;                  /* the listed object */
+    uint32_t target;               /* the object it is meeting */
+    uint32_t start;                /* first step of the meeting */
+    uint32_t end;                  /* the last step's time: the meeting is active */
+    float mbr[4];                  /* low lon, low lat, high lon, high lat */
+} glint_search_info;
+
+/* The reference's active multi-search (search_multi_pid -> search_multi_list,
+ * cuda/geometry.cu:605-663, printed at tracing/process.cpp:465-475), run
+ * against the meeting table after the last step: every meeting active at
+ * that step that has lasted cur_time - start >= min_meet_time + 1 yields
+ * one record per side whose id is listed.  Records come in bucket order, the
+ * lower id's side first; a repeated id counts once (the reference appends
+ * with an atomic counter, so its order is arbitrary).  pids and out are host
+ * arrays; *n receives the number found and the first min(n, cap) records are
+ * written.  Waits for the context's stream.  Returns GLINT_ERR_STATE before
+ * the first step. */
+glint_status glint_active_search(glint_ctx *ctx, const uint32_t *pids, uint32_t npids, glint_search_info *out,
+                                 uint64_t cap, uint64_t *n);
+
 /* ---- synthetic trajectories on the device (benchmark input) ----
  * params/objects: the generator's parameter block and object states as
  * produced by the host generator (glint_pipeline_gb300/csrc/tracegen.h) */

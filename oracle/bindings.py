@@ -74,11 +74,13 @@ SCHEMA_DTYPE = np.dtype([
     ("low", "<f8", (2,)), ("high", "<f8", (2,)), ("children", "<u4", (4,)),
 ])
 assert SCHEMA_DTYPE.itemsize == 80
+# search_info_unit (tracing/workbench.h:85-88)
+SEARCH_DTYPE = np.dtype([("pid", "<u4"), ("target", "<u4"), ("start", "<u4"), ("end", "<u4"), ("mbr", "<f4", (4,))])
+assert SEARCH_DTYPE.itemsize == 32
 
 
 def _load_oracle():
-    if not os.path.exists(ORACLE_SO):
-        build_oracle()
+    build_oracle()  # make: a no-op unless a source is newer than the library
     lib = ctypes.CDLL(ORACLE_SO)
     vp = ctypes.c_void_p
     lib.go_create.restype = vp
@@ -90,6 +92,8 @@ def _load_oracle():
     lib.go_get_meetings.argtypes = [vp, vp, ctypes.c_uint32]
     lib.go_get_schema.argtypes = [vp, vp, vp, vp, vp]
     lib.go_get_buckets.argtypes = [vp, vp, vp, vp, vp]
+    lib.go_active_search.restype = ctypes.c_uint64
+    lib.go_active_search.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_uint64]
     lib.go_dpm_lon.restype = ctypes.c_double
     lib.go_dpm_lon.argtypes = [ctypes.c_double]
     lib.go_sin_cr.restype = ctypes.c_double
@@ -158,6 +162,15 @@ class Oracle:
         m = np.zeros((B, 4), np.float32)
         self.lib.go_get_buckets(self.h, k.ctypes.data, s.ctypes.data, e.ctypes.data, m.ctypes.data)
         return k, s, e, m
+
+    def active_search(self, pids) -> np.ndarray:
+        """Active meetings of the listed objects after the last step
+        (cuda/geometry.cu:605-663), in bucket order."""
+        p = np.ascontiguousarray(pids, dtype=np.uint32)
+        n = self.lib.go_active_search(self.h, p.ctypes.data, p.shape[0], None, 0)
+        out = np.zeros(max(int(n), 1), dtype=SEARCH_DTYPE)
+        self.lib.go_active_search(self.h, p.ctypes.data, p.shape[0], out.ctypes.data, out.shape[0])
+        return out[: int(n)]
 
     def close(self):
         if self.h:

@@ -590,3 +590,41 @@ void go_get_buckets(const go_ctx *c, uint64_t *keys, uint32_t *starts, uint32_t 
     if (ends) memcpy(ends, c->bend, sizeof(uint32_t) * B);
     if (mbrs) memcpy(mbrs, c->bmbr, sizeof(float) * 4 * B);
 }
+
+/* The active multi-search of cuda_identify_meetings (cuda/geometry.cu:
+ * 605-663) over the bucket table as it stands after the last step: a bucket
+ * whose meeting is active (end == cur_time) and has lasted
+ * cur_time - start >= min_meet_time + 1 yields one record per side whose id
+ * is in the list, (listed id, other id, start, end, MBR).  The reference
+ * appends with an atomic counter; here records come in bucket order, the
+ * lower id's side first, and a repeated id in the list counts once. */
+uint64_t go_active_search(const go_ctx *c, const uint32_t *pids, uint32_t npids, go_search_info *out,
+                          uint64_t cap) {
+    const uint32_t N = c->cfg.num_objects;
+    uint8_t *in = (uint8_t *)calloc(N ? N : 1, 1);
+    for (uint32_t i = 0; i < npids; ++i)
+        if (pids[i] < N) in[pids[i]] = 1;
+    uint64_t n = 0;
+    const size_t B = c->cfg.num_meeting_buckets;
+    for (size_t b = 0; b < B; ++b) {
+        if (c->bkey[b] == GO_EMPTY_KEY || c->bend[b] != c->cur_time) continue;
+        if (c->cur_time - c->bstart[b] < c->cfg.min_meet_time + 1) continue;
+        uint32_t a, t;
+        go_cantor_inverse(c->bkey[b], &a, &t);
+        for (int side = 0; side < 2; ++side) {
+            const uint32_t p = side ? t : a, q = side ? a : t;
+            if (p >= N || !in[p]) continue;
+            if (n < cap) {
+                go_search_info *o = out + n;
+                o->pid = p;
+                o->target = q;
+                o->start = c->bstart[b];
+                o->end = c->bend[b];
+                memcpy(o->mbr, c->bmbr + 4 * b, sizeof(float) * 4);
+            }
+            ++n;
+        }
+    }
+    free(in);
+    return n;
+}

@@ -103,6 +103,18 @@ void go_get_schema(const go_ctx *c, go_schema *schema, uint32_t *schema_stack, u
                    uint32_t *grid_counter);
 void go_get_buckets(const go_ctx *c, uint64_t *keys, uint32_t *starts, uint32_t *ends, float *mbrs);
 
+/* search_info_unit (tracing/workbench.h:85-88) */
+typedef struct go_search_info {
+    uint32_t pid, target, start, end;
+    float mbr[4];
+} go_search_info;
+
+/* the GPU path's active multi-search (cuda/geometry.cu:605-663) over the
+ * bucket table after the last step; records in bucket order; returns the
+ * number found (only the first cap are written) */
+uint64_t go_active_search(const go_ctx *c, const uint32_t *pids, uint32_t npids, go_search_info *out,
+                          uint64_t cap);
+
 /* correctly rounded sin on [0, pi/2] by a double-double Taylor series; used to
  * check how often libm's sin differs from the correctly rounded value */
 double go_sin_cr(double x);

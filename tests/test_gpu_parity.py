@@ -104,6 +104,36 @@ def test_parity_precision_form(name):
     run_parity(name, state_every=25, precision_mode=1)
 
 
+@pytest.mark.parametrize("name,precision_mode", [("dense_20k", 0), ("collide_20k", 1), ("reach_8k", 0)])
+def test_active_search_matches_oracle(name, precision_mode):
+    """glint_active_search after a step equals the oracle's restatement of the
+    reference's multi-search, record for record (bucket order, mbr bits)."""
+    box, pts = make_points(name)
+    cfgd = case_config(name)
+    o = Oracle(make_config(**cfgd), box, pts[0])
+    g = DeviceBench(gpu_config(cfgd, precision_mode=precision_mode), box, pts[0])
+    rng = np.random.default_rng(11)
+    found = 0
+    for t in range(pts.shape[0]):
+        o.step(pts[t], t)
+        g.step(pts[t], t)
+        if t % 4 != 3:
+            continue
+        k = 1 + (t % 3) * 500
+        pids = np.concatenate([rng.choice(cfgd["num_objects"], k, replace=False), [1, 1, 2**31]]).astype(np.uint32)
+        want = o.active_search(pids)
+        got = g.active_search(pids)
+        assert got.tobytes() == want.tobytes(), f"step {t}"
+        found += len(got)
+        if len(want) > 3:
+            part = g.active_search(pids, cap=3)
+            assert part.tobytes() == want[:3].tobytes()
+    assert found > 0
+    assert len(g.active_search(np.zeros(0, np.uint32))) == 0
+    g.close()
+    o.close()
+
+
 @pytest.mark.parametrize("name", sorted(CASES))
 def test_gpu_matches_reference_fixtures(name):
     """The GPU's per-step meetings hash to the reference's (tests/golden)."""

@@ -111,3 +111,41 @@ def test_sin_cr_is_correctly_rounded():
     xs = np.concatenate([rng.random(3000) * 1.5707963, 0.838 + rng.random(3000) * 0.008])
     for x in xs:
         assert lib.go_sin_cr(float(x)) == float(mpmath.sin(mpmath.mpf(float(x))))
+
+
+def _search_restated(keys, starts, ends, mbrs, cur, min_meet, pids, n_objects):
+    """numpy restatement of the active multi-search (cuda/geometry.cu:605-663)."""
+    from oracle.bindings import SEARCH_DTYPE, cantor_inverse
+    listed = np.zeros(n_objects, bool)
+    listed[np.asarray(pids)[np.asarray(pids) < n_objects]] = True
+    occ = (keys != (1 << 62)) & (ends == cur) & ((cur - starts.astype(np.int64)) >= min_meet + 1)
+    idx = np.nonzero(occ)[0]
+    a, b = cantor_inverse(keys[idx])
+    rows = []
+    for j, s in enumerate(idx):
+        for p, q in ((a[j], b[j]), (b[j], a[j])):
+            if listed[p]:
+                rows.append((p, q, starts[s], ends[s], mbrs[s]))
+    out = np.zeros(len(rows), SEARCH_DTYPE)
+    for i, r in enumerate(rows):
+        out[i] = r
+    return out
+
+
+def test_oracle_active_search_restated():
+    """The oracle's active search equals a direct restatement over its buckets."""
+    box, pts = make_points("dense_20k", 20)
+    cfgd = case_config("dense_20k")
+    o = Oracle(make_config(**cfgd), box, pts[0])
+    rng = np.random.default_rng(7)
+    for t in range(pts.shape[0]):
+        o.step(pts[t], t)
+        if t < 8:
+            continue
+        pids = np.concatenate([rng.choice(cfgd["num_objects"], 400, replace=False), [0, 0, 10**9]]).astype(np.uint32)
+        got = o.active_search(pids)
+        k, s, e, m = o.buckets()
+        want = _search_restated(k, s, e, m, t, cfgd["min_meet_time"], pids, cfgd["num_objects"])
+        assert len(want) > 0
+        np.testing.assert_array_equal(got.view(np.uint8), want.view(np.uint8))
+    o.close()
