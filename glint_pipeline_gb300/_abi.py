@@ -141,6 +141,7 @@ def load_library(path: str | None = None):
     lib.glint_stream.restype = vp
     lib.glint_stream.argtypes = [vp]
     lib.glint_active_search.argtypes = [vp, vp, u32, vp, u64, ctypes.POINTER(u64)]
+    lib.glint_active_search_noalloc.argtypes = [vp, vp, u32, vp, u64, vp]
     lib.glint_gen_create.argtypes = [vp, u32, vp, u32, u32, u32, ctypes.POINTER(vp)]
     lib.glint_gen_step.argtypes = [vp, vp, vp]
     lib.glint_gen_destroy.argtypes = [vp]

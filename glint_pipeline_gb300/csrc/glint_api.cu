@@ -27,6 +27,7 @@ void refine_prec_set_attributes(uint32_t cap);
 void schema_set_attributes();
 size_t refine_smem_bytes(uint32_t cap);
 uint64_t identify_tiles(uint64_t B);
+cudaError_t noalloc_setup(int device);
 } // namespace glint
 
 using namespace glint;
@@ -469,6 +470,9 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     cudaMemsetAsync(c->d_stamp, 0, c->B + 16, c->stream);
     cudaMemsetAsync(c->d_grid_count, 0, sizeof(uint32_t) * ((size_t)G + 1), c->stream);
     k_iota<<<grid_for(N, 256, 152u * 8u), 256, 0, c->stream>>>(c->d_order, N);
+    /* scratch address of glint_active_search_noalloc, once per device, with
+     * this device current; a failure is reported by that call */
+    noalloc_setup(c->device);
     partition_set_attributes();
     refine_set_attributes(c->cap);
     refine_prec_set_attributes(c->cap);

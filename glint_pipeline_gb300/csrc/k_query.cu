@@ -17,6 +17,7 @@
  */
 #include <algorithm>
 #include <cstring>
+#include <mutex>
 
 #include "glint_internal.cuh"
 
@@ -234,5 +235,120 @@ extern "C" glint_status glint_active_search(glint_ctx *c, const uint32_t *pids, 
         return e == cudaErrorMemoryAllocation ? GLINT_ERR_OUT_OF_MEMORY : GLINT_ERR_CUDA;
     }
     if (n) *n = found;
+    return GLINT_OK;
+}
+
+/* ---- allocation-free variant --------------------------------------------
+ * glint_active_search_noalloc takes device arrays and keeps its scratch in
+ * one fixed-size device array of this library: the id bitmap (objects up to
+ * kNaMaxObjects) and the per-tile counts and offsets (buckets up to
+ * kNaMaxTiles * 8192).  Its address is looked up once per device while a
+ * context is created on it; the call itself allocates nothing. */
+namespace glint {
+
+constexpr uint32_t kNaMaxObjects = 1u << 24;                 /* 16.7M objects: 2 MB of bits */
+constexpr uint32_t kNaMaxTiles = 1u << 17;                   /* 2^30 buckets: 2 x 512 KB */
+constexpr size_t kNaBitsWords = kNaMaxObjects / 32;
+constexpr size_t kNaTileWords = (size_t)kNaMaxTiles + 64;    /* tiles + 1, padded to 256 B */
+constexpr size_t kNaWords = kNaBitsWords + 2 * kNaTileWords;
+constexpr int kNaMaxDevices = 64;
+
+static __device__ __align__(256) uint32_t g_noalloc_scratch[kNaWords];
+
+std::mutex g_na_mutex;
+uint32_t *g_na_ptr[kNaMaxDevices];
+cudaError_t g_na_status[kNaMaxDevices];
+bool g_na_done[kNaMaxDevices];
+
+/* exclusive scan of n (<= kNaMaxTiles + 1) values by one block, no scratch */
+__global__ void __launch_bounds__(1024) k_scan_one_block(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
+                                                         uint64_t n) {
+    __shared__ uint32_t ws[32];
+    __shared__ uint32_t carry;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint64_t base = 0; base < n; base += blockDim.x) {
+        const uint64_t i = base + threadIdx.x;
+        const uint32_t v = i < n ? in[i] : 0u;
+        uint32_t x = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += y;
+        }
+        if (lane == 31) ws[wid] = x;
+        __syncthreads();
+        if (wid == 0) {
+            uint32_t s = ws[lane];
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
+                if (lane >= o) s += y;
+            }
+            ws[lane] = s;
+        }
+        __syncthreads();
+        const uint32_t excl = carry + (wid ? ws[wid - 1] : 0u) + x - v;
+        if (i < n) out[i] = excl;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += ws[31];
+        __syncthreads();
+    }
+}
+
+/* looks up the scratch address on the current device, once per device */
+cudaError_t noalloc_setup(int device) {
+    if (device < 0 || device >= kNaMaxDevices) return cudaErrorInvalidDevice;
+    std::lock_guard<std::mutex> lock(g_na_mutex);
+    if (!g_na_done[device]) {
+        void *p = nullptr;
+        g_na_status[device] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        g_na_ptr[device] = g_na_status[device] == cudaSuccess ? static_cast<uint32_t *>(p) : nullptr;
+        g_na_done[device] = true;
+    }
+    return g_na_status[device];
+}
+
+} // namespace glint
+
+extern "C" glint_status glint_active_search_noalloc(glint_ctx *c, const uint32_t *d_pids, uint32_t npids,
+                                                    glint_search_info *d_out, uint64_t cap, uint64_t *d_n) {
+    if (!c || (npids && !d_pids) || (cap && !d_out) || !d_n) return GLINT_ERR_INVALID_ARGUMENT;
+    if (c->step_index == 0) {
+        c->last_error = "active search before the first step";
+        return GLINT_ERR_STATE;
+    }
+    if (c->N > kNaMaxObjects || identify_tiles(c->B) > kNaMaxTiles) {
+        c->last_error = "glint_active_search_noalloc: context larger than its fixed scratch (objects <= 2^24, "
+                        "buckets <= 2^30); use glint_active_search";
+        return GLINT_ERR_UNSUPPORTED;
+    }
+    uint32_t *base = nullptr;
+    cudaError_t st = cudaErrorInvalidDevice;
+    {
+        std::lock_guard<std::mutex> lock(g_na_mutex);
+        if (c->device >= 0 && c->device < kNaMaxDevices && g_na_done[c->device]) {
+            st = g_na_status[c->device];
+            base = g_na_ptr[c->device];
+        }
+    }
+    if (st != cudaSuccess || !base) {
+        c->last_error = std::string("glint_active_search_noalloc: scratch lookup failed: ") + cudaGetErrorString(st);
+        return GLINT_ERR_CUDA;
+    }
+    cudaSetDevice(c->device);
+    uint32_t *bits = base;
+    uint32_t *tile_cnt = base + kNaBitsWords;
+    uint32_t *tile_off = tile_cnt + kNaTileWords;
+    auto scan = [](const uint32_t *in, uint32_t *o, uint64_t m, cudaStream_t s) {
+        k_scan_one_block<<<1, 1024, 0, s>>>(in, o, m + 1);
+        return cudaGetLastError();
+    };
+    static_assert(sizeof(uint64_t) == sizeof(unsigned long long), "u64");
+    const cudaError_t e = launch_active_search(c, bits, tile_cnt, tile_off, scan, d_pids, npids, d_out, cap,
+                                               reinterpret_cast<unsigned long long *>(d_n));
+    if (e != cudaSuccess) {
+        c->last_error = std::string("glint_active_search_noalloc: ") + cudaGetErrorString(e);
+        return GLINT_ERR_CUDA;
+    }
     return GLINT_OK;
 }

@@ -224,6 +224,23 @@ typedef struct glint_search_info {
 glint_status glint_active_search(glint_ctx *ctx, const uint32_t *pids, uint32_t npids, glint_search_info *out,
                                  uint64_t cap, uint64_t *n);
 
+/* No counterpart in the reference: glint_active_search for callers that must
+ * not allocate device memory on the call (a serving loop, a captured
+ * stream).  d_pids (npids ids), d_out (cap records) and d_n (one uint64_t
+ * receiving the count) are device arrays; the same records as
+ * glint_active_search are written to d_out.  Enqueued on the context's stream
+ * (glint_stream); returns without waiting.
+ * Scratch: one fixed array of the library per device (2 MB id bitmap +
+ * 1 MB of tile counters), whose address is looked up once per device inside
+ * glint_create with that device current; the call itself performs no
+ * allocation.  The bitmap is cleared by each call; nothing else needs to
+ * start at zero.  Limits: contexts of at most 2^24 objects and 2^30 buckets
+ * (GLINT_ERR_UNSUPPORTED otherwise).  Calls that overlap in time on the same
+ * device (from any context or stream) share the scratch and race: order them
+ * on one stream or synchronise between them. */
+glint_status glint_active_search_noalloc(glint_ctx *ctx, const uint32_t *d_pids, uint32_t npids,
+                                         glint_search_info *d_out, uint64_t cap, uint64_t *d_n);
+
 /* ---- synthetic trajectories on the device (benchmark input) ----
  * params/objects: the generator's parameter block and object states as
  * produced by the host generator (glint_pipeline_gb300/csrc/tracegen.h) */
