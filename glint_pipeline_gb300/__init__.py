@@ -59,6 +59,9 @@ class Configuration:
     meeting_log_capacity: int = 0
     timing: bool = False
     auto_flush: bool = False
+    split_num: int = 10
+    kv_restriction: int = 0             # 0 -> G_bytes * 2^25 keys (config.h:80)
+    kv_capacity: int = 0                # 0 -> kv_restriction + 1000000 (config.h:81)
 
     def to_c(self) -> GlintConfig:
         c = GlintConfig()
@@ -159,6 +162,38 @@ class DeviceBench:
         if st != 0:
             raise GlintError(st, self.last_error())
         return out[: min(int(n.value), int(cap))]
+
+    # -- key-value store -----------------------------------------------------
+    def flush(self) -> "_abi.GlintStoreInfo":
+        """Flush the pending keys into the store now (cuda/geometry.cu:1752-2135)."""
+        info = _abi.GlintStoreInfo()
+        st = self.lib.glint_flush(self.h, ctypes.byref(info))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        return info
+
+    def store(self) -> dict:
+        """The last flush's store as host arrays (the reference's h_keys,
+        h_sids, h_CTF_capacity, h_ctfs, h_bitmaps and oversize buffer)."""
+        info = _abi.GlintStoreInfo()
+        st = self.lib.glint_store_read(self.h, None, None, None, None, None, None, None, None, ctypes.byref(info))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        C = self.config.CTF_count or 100
+        out = {"keys": np.zeros(int(info.key_bytes), np.uint8), "sids": np.zeros(self.n, np.uint16),
+               "ctf_capacity": np.zeros(C, np.uint32), "ctfs": np.zeros(C, _abi.CTF_META_DTYPE),
+               "bitmaps": np.zeros(C * _abi.BITMAP_BYTES, np.uint8),
+               "o_keys": np.zeros((int(info.oversize_kv_count), 16), np.uint8),
+               "o_boxes": np.zeros((int(info.oversize_kv_count), 4), np.float32),
+               "o_bitmap": np.zeros(_abi.BITMAP_BYTES, np.uint8)}
+        ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        st = self.lib.glint_store_read(self.h, ptr(out["keys"]), ptr(out["sids"]), ptr(out["ctf_capacity"]),
+                                       ptr(out["ctfs"]), ptr(out["bitmaps"]), ptr(out["o_keys"]),
+                                       ptr(out["o_boxes"]), ptr(out["o_bitmap"]), ctypes.byref(info))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        out["info"] = info
+        return out
 
     # -- state ------------------------------------------------------------------
     def schema(self):

@@ -49,7 +49,10 @@ class GlintConfig(ctypes.Structure):
         ("meeting_log_capacity", ctypes.c_uint64),
         ("timing", ctypes.c_uint32),
         ("auto_flush", ctypes.c_uint32),
-        ("reserved", ctypes.c_uint32 * 6),
+        ("split_num", ctypes.c_uint32),
+        ("reserved0", ctypes.c_uint32),
+        ("kv_restriction", ctypes.c_uint64),
+        ("kv_capacity", ctypes.c_uint64),
     ]
 
 
@@ -93,6 +96,9 @@ class GlintStepStats(ctypes.Structure):
         ("launches", ctypes.c_uint32),
         ("meeting_log_size", ctypes.c_uint64),
         ("ms", ctypes.c_float * 8),
+        ("kv_count", ctypes.c_uint64),
+        ("flushed", ctypes.c_uint32),
+        ("flush_ms", ctypes.c_float),
     ]
 
     def as_dict(self):
@@ -108,6 +114,29 @@ SCHEMA_DTYPE = np.dtype([
     ("low", "<f8", (2,)), ("high", "<f8", (2,)), ("children", "<u4", (4,)),
 ])
 assert SCHEMA_DTYPE.itemsize == 80 and MEETING_DTYPE.itemsize == 32
+# glint_ctf_meta: CTF (tracing/step_merge.h) without its pointers
+CTF_META_DTYPE = np.dtype([("ctf_mbr", "<f4", (4,)), ("CTF_kv_capacity", "<u4"), ("start_time_min", "<u4"),
+                           ("start_time_max", "<u4"), ("end_time_min", "<u4"), ("end_time_max", "<u4"),
+                           ("ctf_bitmap_size", "<u4"), ("key_bit", "<u2"), ("id_bit", "<u2"),
+                           ("duration_bit", "<u2"), ("end_bit", "<u2"), ("low_x_bit", "<u2"), ("low_y_bit", "<u2"),
+                           ("edge_bit", "<u2"), ("mbr_bit", "<u2"), ("x_grid", "<u2"), ("y_grid", "<u2"),
+                           ("reserved", "<u4")])
+assert CTF_META_DTYPE.itemsize == 64
+BITMAP_BYTES = 256 * 256 // 8
+
+
+class GlintStoreInfo(ctypes.Structure):
+    _fields_ = [("kv_count", ctypes.c_uint64), ("key_bytes", ctypes.c_uint64), ("oversize_kv_count", ctypes.c_uint32),
+                ("oversize_start_time_min", ctypes.c_uint32), ("oversize_start_time_max", ctypes.c_uint32),
+                ("oversize_end_time_min", ctypes.c_uint32), ("oversize_end_time_max", ctypes.c_uint32),
+                ("sid_count", ctypes.c_uint32), ("oversize_oid_count", ctypes.c_uint32),
+                ("end_time_min", ctypes.c_uint32), ("cur_time", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("bits_outside", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 # glint_search_info = search_info_unit (tracing/workbench.h:85-88)
 SEARCH_DTYPE = np.dtype([("pid", "<u4"), ("target", "<u4"), ("start", "<u4"), ("end", "<u4"), ("mbr", "<f4", (4,))])
 assert SEARCH_DTYPE.itemsize == 32
@@ -141,6 +170,8 @@ def load_library(path: str | None = None):
     lib.glint_stream.restype = vp
     lib.glint_stream.argtypes = [vp]
     lib.glint_active_search.argtypes = [vp, vp, u32, vp, u64, ctypes.POINTER(u64)]
+    lib.glint_flush.argtypes = [vp, ctypes.POINTER(GlintStoreInfo)]
+    lib.glint_store_read.argtypes = [vp] * 9 + [ctypes.POINTER(GlintStoreInfo)]
     lib.glint_active_search_noalloc.argtypes = [vp, vp, u32, vp, u64, vp]
     lib.glint_gen_create.argtypes = [vp, u32, vp, u32, u32, u32, ctypes.POINTER(vp)]
     lib.glint_gen_step.argtypes = [vp, vp, vp]

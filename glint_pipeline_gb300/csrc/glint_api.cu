@@ -178,9 +178,12 @@ void free_all(glint_ctx *c) {
                     c->d_scan_tmp, c->d_qbits, c->d_qpids, c->d_qout, c->d_qn};
     for (void *p : ptrs)
         if (p) cudaFree(p);
+    flush_free(c);
     if (c->h_cnt) cudaFreeHost(c->h_cnt);
-    if (c->timers.created)
+    if (c->timers.created) {
         for (auto &e : c->timers.ev) cudaEventDestroy(e);
+        for (auto &e : c->flush_ev) cudaEventDestroy(e);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -208,7 +211,7 @@ Frame make_frame(const glint_box &mbr, const glint_schema_node &root, double r, 
 }
 
 void to_device_nodes(const glint_schema_node *in, uint32_t n, const Frame &f, std::vector<DNode> &dn,
-                     std::vector<double2> &lo, std::vector<longlong4> &ib) {
+                     std::vector<double2> &lo, std::vector<IBox> &ib) {
     for (uint32_t i = 0; i < n; ++i) {
         DNode d;
         std::memset(&d, 0, sizeof(d));
@@ -273,6 +276,7 @@ void glint_config_defaults(glint_config *cfg, uint32_t n) {
     cfg->CTF_count = 100;
     cfg->dProbFalse = 100;
     cfg->precision_mode = 0;
+    cfg->split_num = 10;
 }
 
 glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, const double *first_points,
@@ -286,6 +290,12 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     if (!init && !first_points) return GLINT_ERR_INVALID_ARGUMENT;
     if (cfg.num_meeting_buckets == 0) cfg.num_meeting_buckets = 2ull * cfg.num_objects;
     if (cfg.schema_update_delay == 0) cfg.schema_update_delay = 1;
+    if (cfg.CTF_count == 0) cfg.CTF_count = 100;
+    if (cfg.split_num == 0) cfg.split_num = 10;
+    if (cfg.G_bytes == 0) cfg.G_bytes = 2;
+    if (cfg.max_meet_time == 0) cfg.max_meet_time = 4096;
+    /* make_sid numbers split_num^2 cells: one CTF each */
+    if (cfg.CTF_count != cfg.split_num * cfg.split_num || cfg.split_num > 64) return GLINT_ERR_UNSUPPORTED;
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return GLINT_ERR_NO_DEVICE;
     if ((int)cfg.device >= ndev) return GLINT_ERR_INVALID_ARGUMENT;
@@ -317,13 +327,19 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     c->dpm_lat = 360.0 / (40076.0 * 1000.0);
     c->x_buffer = cfg.x_buffer != 0 ? cfg.x_buffer : cfg.reach_distance * h_dpm_lon(mbr->low[1]);
     c->y_buffer = cfg.y_buffer != 0 ? cfg.y_buffer : cfg.reach_distance * c->dpm_lat;
+    /* key-value store sizes (util/config.h:77-85) and the first window */
+    c->kv_restriction = cfg.kv_restriction ? cfg.kv_restriction : (uint64_t)cfg.G_bytes * 33554432ull;
+    c->kv_cap = cfg.kv_capacity ? cfg.kv_capacity : c->kv_restriction + 1000000;
+    c->end_time_min = cfg.start_time + cfg.min_meet_time; /* tracing/process.cpp:404 */
     /* decisions within 2^-38 relative of the threshold are re-taken exactly */
     c->band = cfg.reach_distance * std::ldexp(1.0, -38);
     if (c->cap == 0 || c->cap > 4096) { delete c; return GLINT_ERR_UNSUPPORTED; }
 
     const uint32_t G = c->G, S = c->S;
     c->n_tiles = identify_tiles(c->B);
-    const size_t scan_n = std::max<size_t>({(size_t)N, (size_t)G, (size_t)S, (size_t)c->n_tiles}) + 1;
+    /* scans: objects, grids, slots, identify tiles and radix-sort digit tables */
+    const size_t radix_n = 256 * (((size_t)N + 1023) / 1024) + 1;
+    const size_t scan_n = std::max<size_t>({(size_t)N, (size_t)G, (size_t)S, (size_t)c->n_tiles, radix_n}) + 1;
     c->scan_tmp_bytes = scan_tmp_bytes(scan_n);
 #define ALLOC(ptr, count)                                                  \
     do {                                                                   \
@@ -391,6 +407,12 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
         c->d_scan_tmp = tmp;
     }
 #undef ALLOC
+    if ((e = flush_alloc(c)) != cudaSuccess) {
+        glint_status st = cuda_fail(c, e, "key-value store");
+        free_all(c);
+        delete c;
+        return st;
+    }
     if ((e = cudaMallocHost((void **)&c->h_cnt, sizeof(DevCounters))) != cudaSuccess) {
         glint_status st = cuda_fail(c, e, "cudaMallocHost");
         free_all(c);
@@ -451,11 +473,11 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     c->frame = make_frame(*mbr, sch[0], cfg.reach_distance, c->dpm_lat);
     std::vector<DNode> dn(S);
     std::vector<double2> lo(S);
-    std::vector<longlong4> ib(S);
+    std::vector<IBox> ib(S);
     to_device_nodes(sch.data(), S, c->frame, dn, lo, ib);
     cudaMemcpy(c->d_nodes, dn.data(), sizeof(DNode) * S, cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_low, lo.data(), sizeof(double2) * S, cudaMemcpyHostToDevice);
-    cudaMemcpy(c->d_ibox, ib.data(), sizeof(longlong4) * S, cudaMemcpyHostToDevice);
+    cudaMemcpy(c->d_ibox, ib.data(), sizeof(IBox) * S, cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_sstack, sstack.data(), sizeof(uint32_t) * S, cudaMemcpyHostToDevice);
     cudaMemcpy(c->d_gstack, gstack.data(), sizeof(uint32_t) * G, cudaMemcpyHostToDevice);
     DevCounters hc;
@@ -477,7 +499,9 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     refine_set_attributes(c->cap);
     refine_prec_set_attributes(c->cap);
     schema_set_attributes();
+    flush_set_attributes();
     for (auto &ev : c->timers.ev) cudaEventCreate(&ev);
+    for (auto &ev : c->flush_ev) cudaEventCreate(&ev);
     c->timers.created = true;
     e = cudaStreamSynchronize(c->stream);
     if (e == cudaSuccess) e = cudaGetLastError();
@@ -535,6 +559,7 @@ static glint_status enqueue_step(glint_ctx *c, const double *points, bool host, 
     launch_insert(c, cur_time);
     if (tm) cudaEventRecord(c->timers.ev[5], s);
     launch_identify(c, cur_time);
+    launch_keys(c);
     if (tm) cudaEventRecord(c->timers.ev[6], s);
     if (c->cfg.dynamic_schema) launch_schema_update(c);
     k_step_tail<<<1, 1, 0, s>>>(c->d_qstart, c->N, c->d_cnt);
@@ -569,9 +594,12 @@ static void fill_stats(glint_ctx *c, glint_step_stats *st) {
     st->band_pairs = h.band_pairs;
     st->error_flags = h.error_flags;
     /* kernels per step: partition 9, filter 9, refine 1, insert 1,
-     * identify 6, schema update 11, tail 1 (scans count three each) */
-    st->launches = 9 + 9 + 1 + 1 + 6 + (c->cfg.dynamic_schema ? 11 : 0) + 1;
+     * identify 6 + keys 1, schema update 11, tail 1 (scans count three each) */
+    st->launches = 9 + 9 + 1 + 1 + 7 + (c->cfg.dynamic_schema ? 11 : 0) + 1;
     st->meeting_log_size = h.log_head;
+    st->kv_count = h.kv_count;
+    st->flushed = c->last_flushed ? 1u : 0u;
+    st->flush_ms = c->last_flush_ms;
     if (c->cfg.timing) {
         for (int k = 0; k < 7; ++k) cudaEventElapsedTime(&st->ms[k], c->timers.ev[k], c->timers.ev[k + 1]);
         cudaEventElapsedTime(&st->ms[7], c->timers.ev[0], c->timers.ev[7]);
@@ -582,12 +610,34 @@ glint_status glint_sync(glint_ctx *c, glint_step_stats *st) {
     if (!c) return GLINT_ERR_INVALID_ARGUMENT;
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "sync");
+    if (!c->stats_valid) {
+        c->last_flushed = false;
+        c->last_flush_ms = 0;
+    }
+    if (c->cfg.auto_flush && !c->stats_valid && c->h_cnt->kv_count > c->kv_restriction &&
+        !(c->h_cnt->error_flags & GLINT_EF_KV_OVERFLOW)) {
+        /* the reference flushes inside the step once kv_count passes
+         * kv_restriction (cuda/geometry.cu:1752) */
+        cudaEventRecord(c->flush_ev[0], c->stream);
+        std::string err;
+        const glint_status fs = run_flush(c, nullptr, err);
+        cudaEventRecord(c->flush_ev[1], c->stream);
+        cudaEventSynchronize(c->flush_ev[1]);
+        if (fs != GLINT_OK) {
+            c->last_error = err;
+            return fs;
+        }
+        cudaEventElapsedTime(&c->last_flush_ms, c->flush_ev[0], c->flush_ev[1]);
+        c->last_flushed = true;
+        cudaMemcpy(c->h_cnt, c->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost);
+    }
     fill_stats(c, &c->last_stats);
     c->stats_valid = true;
     if (st) *st = c->last_stats;
     if (c->last_stats.error_flags & (GLINT_EF_CHECKS_OVERFLOW | GLINT_EF_NEW_OVERFLOW | GLINT_EF_TABLE_FULL |
                                      GLINT_EF_SCHEMA_STACK | GLINT_EF_SEGMENT_TOO_LARGE | GLINT_EF_DFS_OVERFLOW |
-                                     GLINT_EF_DUPLICATE_NEW | GLINT_EF_TREE_DEPTH | GLINT_EF_LOG_OVERFLOW)) {
+                                     GLINT_EF_DUPLICATE_NEW | GLINT_EF_TREE_DEPTH | GLINT_EF_LOG_OVERFLOW |
+                                     GLINT_EF_KV_OVERFLOW | GLINT_EF_STORE_DOMAIN)) {
         char buf[96];
         std::snprintf(buf, sizeof(buf), "capacity or consistency error, flags 0x%x", c->last_stats.error_flags);
         c->last_error = buf;

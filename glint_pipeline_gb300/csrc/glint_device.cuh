@@ -309,6 +309,11 @@ struct Frame {
 
 constexpr double kFxLimit = 1152921504606846976.0; /* 2^60 */
 
+/* a node box in fixed point: low x, low y, high x, high y */
+struct __align__(32) IBox {
+    long long x, y, z, w;
+};
+
 __host__ __device__ inline long long fx_coord(double v, double o, double S, bool *clamped) {
     double t = (v - o) * S; /* S is a power of two: the product is exact */
     bool c = false;
@@ -370,8 +375,8 @@ __device__ inline int fx_screen(long long dx, long long dy, const Screen &s, flo
     return -1;
 }
 
-__host__ __device__ inline longlong4 fx_box(double lx, double ly, double hx, double hy, const Frame &f) {
-    longlong4 b;
+__host__ __device__ inline IBox fx_box(double lx, double ly, double hx, double hy, const Frame &f) {
+    IBox b;
     b.x = fx_coord(lx, f.ox, f.S, nullptr);
     b.y = fx_coord(ly, f.oy, f.S, nullptr);
     b.z = fx_coord(hx, f.ox, f.S, nullptr);
@@ -380,7 +385,7 @@ __host__ __device__ inline longlong4 fx_box(double lx, double ly, double hx, dou
 }
 
 /* box distance screening: the gap from the point to the box along each axis */
-__device__ inline int fx_box_screen(const longlong4 &b, long long px, long long py, const Screen &s, float cy) {
+__device__ inline int fx_box_screen(const IBox &b, long long px, long long py, const Screen &s, float cy) {
     long long dx = b.x - px;
     if (px - b.z > dx) dx = px - b.z;
     if (dx < 0) dx = 0;

@@ -23,6 +23,7 @@
 
 #include <cuda_runtime.h>
 #include <string>
+#include <vector>
 
 #include "glint_device.cuh"
 
@@ -58,6 +59,11 @@ struct DevCounters {
     unsigned int gsi;                      /* grids_stack_index */
     unsigned long long log_head;           /* meetings written to the log so far */
     unsigned long long log_step_begin;     /* log position of this step's first meeting */
+    unsigned long long kv_count;           /* keys pending for the next flush */
+    unsigned int sid_count;                /* objects with at least one pending key */
+    unsigned int oversize_oid_count;
+    unsigned int keys_outside;             /* meetings outside the map box (not keyed) */
+    unsigned int pad2[3];
 };
 /* bytes cleared at the start of every step */
 constexpr size_t kStepCounterBytes = offsetof(DevCounters, ssi);
@@ -109,7 +115,7 @@ struct glint_ctx {
     float2 *d_sfpos = nullptr;             /* [N] sorted f32 coordinates (meeting boxes) */
     float *d_sc = nullptr;                 /* [N] sorted metres per unit along x */
     float2 *d_fpos = nullptr;              /* [N] f32 coordinates by object id */
-    longlong4 *d_ibox = nullptr;           /* [S] fixed-point node boxes */
+    glint::IBox *d_ibox = nullptr;           /* [S] fixed-point node boxes */
     glint::Frame frame;
     uint32_t *d_leaf_work = nullptr;       /* [G] grid ids with objects */
 
@@ -145,6 +151,35 @@ struct glint_ctx {
     /* output */
     glint_meeting *d_log = nullptr;
 
+    /* key-value store (k_flush.cu) */
+    uint64_t kv_cap = 0, kv_restriction = 0;
+    uint32_t end_time_min = 0;
+    ulonglong2 *d_keys = nullptr, *d_keys2 = nullptr;   /* 128-bit keys, pending / sorted */
+    float4 *d_kvbox = nullptr, *d_kvbox2 = nullptr;
+    uint32_t *d_same = nullptr;            /* [N] same_pid_count */
+    uint4 *d_obox = nullptr;               /* [N] o_boxs */
+    uint16_t *d_sids = nullptr, *d_sids_out = nullptr;
+    uint8_t *d_over = nullptr;
+    uint32_t *d_oids = nullptr, *d_oids2 = nullptr;
+    unsigned long long *d_mid = nullptr, *d_mid2 = nullptr;
+    uint32_t *d_gcount = nullptr, *d_gstart = nullptr, *d_segof = nullptr, *d_segcur = nullptr, *d_segbig = nullptr;
+    uint32_t *d_ctf_cap = nullptr, *d_ctf_n = nullptr;
+    glint_ctf_meta *d_ctfs = nullptr;
+    unsigned long long *d_ctf_lo = nullptr, *d_ctf_byte = nullptr;
+    uint8_t *d_ctf_keys = nullptr, *d_bitmaps = nullptr, *d_obitmap = nullptr;
+    unsigned long long *d_fmisc = nullptr;
+    void *d_rs_tmp = nullptr;
+    glint_store_info store;
+    std::vector<uint32_t> store_ctf_cap;
+    bool store_valid = false;
+    ulonglong2 *store_keys_ptr = nullptr;
+    float4 *store_boxes_ptr = nullptr;
+    uint64_t store_kv = 0;
+    uint32_t flushes = 0;
+    cudaEvent_t flush_ev[2];
+    float last_flush_ms = 0;
+    bool last_flushed = false;
+
     /* active search scratch, allocated on first use */
     uint32_t *d_qbits = nullptr;
     uint32_t *d_qpids = nullptr;
@@ -179,6 +214,11 @@ cudaError_t launch_refine(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_insert(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_identify(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_schema_update(glint_ctx *c);
+cudaError_t launch_keys(glint_ctx *c);
+cudaError_t flush_alloc(glint_ctx *c);
+void flush_free(glint_ctx *c);
+void flush_set_attributes();
+glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err);
 
 inline ExactCtx make_exact(glint_ctx *c) {
     ExactCtx e;

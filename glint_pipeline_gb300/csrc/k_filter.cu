@@ -54,7 +54,7 @@ __device__ inline WalkPoint walk_point(const double2 p, const longlong2 ip, floa
  * reference's FP64 box distance. */
 template <class Emit>
 __device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const double2 *__restrict__ low,
-                                       const longlong4 *__restrict__ ibox, uint32_t start, const WalkPoint &w,
+                                       const IBox *__restrict__ ibox, uint32_t start, const WalkPoint &w,
                                        const Frame &f, const ExactCtx &ex, DevCounters *cnt, Emit emit) {
     uint32_t st_node[kStackMax];
     uint8_t st_next[kStackMax];
@@ -110,7 +110,7 @@ struct FilterArgs {
     const uint32_t *obj_leaf;
     const DNode *nodes;
     const double2 *low;
-    const longlong4 *ibox;
+    const IBox *ibox;
     uint32_t N;
     Frame f;
     ExactCtx ex;

@@ -353,7 +353,7 @@ __global__ void __launch_bounds__(256) k_sch_apply_merge(DNode *__restrict__ nod
 }
 
 __global__ void __launch_bounds__(256) k_sch_apply_split(DNode *__restrict__ nodes, double2 *__restrict__ low,
-                                                         longlong4 *__restrict__ ibox, Frame fr,
+                                                         IBox *__restrict__ ibox, Frame fr,
                                                          const uint8_t *__restrict__ flags,
                                                          const uint32_t *__restrict__ events, const uint4 *evdata,
                                                          uint32_t *__restrict__ grid_count, const DevCounters *cnt) {

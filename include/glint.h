@@ -58,6 +58,8 @@ typedef enum glint_status {
 #define GLINT_EF_DFS_OVERFLOW        0x0080u /* lookup depth beyond the supported tree depth */
 #define GLINT_EF_SCHEMA_WINDOW       0x0100u /* schema update took the slow path */
 #define GLINT_EF_TREE_DEPTH          0x0200u /* descent deeper than the supported tree depth */
+#define GLINT_EF_KV_OVERFLOW         0x0400u /* more keys pending than kv_capacity */
+#define GLINT_EF_STORE_DOMAIN        0x0800u /* a flush outside the reference's domain (see glint_flush) */
 
 /* The configuration fields this path reads from the reference's
  * `configuration` (util/config.h:15-114), plus this implementation's own. */
@@ -85,8 +87,12 @@ typedef struct glint_config {
     uint64_t check_capacity;       /* cross-leaf check buffer (entries); 0 -> automatic */
     uint64_t meeting_log_capacity; /* meetings kept on device until the next flush; 0 -> automatic */
     uint32_t timing;               /* 1: record per-stage CUDA-event times in glint_step_stats.ms */
-    uint32_t auto_flush;           /* 1: flush when the log passes kv_restriction keys, as geometry.cu:1752 */
-    uint32_t reserved[6];
+    uint32_t auto_flush;           /* 1: flush inside the step once more than kv_restriction keys are
+                                      pending, as cuda/geometry.cu:1752 */
+    uint32_t split_num;            /* configuration::split_num (10): STR slices per axis */
+    uint32_t reserved0;
+    uint64_t kv_restriction;       /* 0 -> G_bytes*2^25 keys (util/config.h:80) */
+    uint64_t kv_capacity;          /* key buffer; 0 -> kv_restriction + 1000000 (util/config.h:81) */
 } glint_config;
 
 typedef struct glint_box {
@@ -151,8 +157,11 @@ typedef struct glint_step_stats {
     uint32_t band_pairs;           /* precision mode: pairs inside the FP32 guard band */
     uint32_t error_flags;          /* GLINT_EF_* */
     uint32_t launches;             /* kernels the step launched */
-    uint64_t meeting_log_size;     /* meetings held on device for the next flush */
+    uint64_t meeting_log_size;     /* meetings written to the device log so far */
     float ms[8];                   /* copy, partition, filter, refine, insert, identify, schema, total */
+    uint64_t kv_count;             /* keys pending for the next flush (workbench::kv_count) */
+    uint32_t flushed;              /* 1: this step ended with an automatic flush */
+    float flush_ms;                /* its device time (not included in ms[7]) */
 } glint_step_stats;
 
 typedef struct glint_ctx glint_ctx;
@@ -199,6 +208,57 @@ glint_status glint_get_capacities(const glint_ctx *ctx, uint32_t *schema_capacit
                                   uint64_t *buckets);
 /* the context's cudaStream_t */
 void *glint_stream(glint_ctx *ctx);
+
+/* ---- flush into the sorted key-value + bitmap store ------------------------
+ * Every identified meeting whose box lies inside the map becomes two keys
+ * (cuda/geometry.cu:665-734): [sid:12][pid:26][target:26][duration:32]
+ * [end - end_time_min:32], one per direction, with its f32 box.  A flush
+ * (cuda/geometry.cu:1752-2135) partitions objects into CTF_count files by an
+ * STR split of their mean positions, sorts the keys, and packs each file's
+ * keys into key_bit/8 bytes with the box quantised to the file's extent
+ * (tracing/step_merge.cpp:132-186); objects whose meetings lasted longer than
+ * max_meet_time or whose area exceeds dProbFalse go to the oversize buffer. */
+
+/* CTF (tracing/step_merge.h) without its two pointers, 64 bytes */
+typedef struct glint_ctf_meta {
+    float ctf_mbr[4];              /* low lon, low lat, high lon, high lat */
+    uint32_t CTF_kv_capacity;
+    uint32_t start_time_min, start_time_max;
+    uint32_t end_time_min, end_time_max;
+    uint32_t ctf_bitmap_size;      /* bytes */
+    uint16_t key_bit, id_bit, duration_bit, end_bit, low_x_bit, low_y_bit, edge_bit, mbr_bit, x_grid, y_grid;
+    uint32_t reserved;
+} glint_ctf_meta;
+
+typedef struct glint_store_info {
+    uint64_t kv_count;             /* keys in the CTFs (h_CTF_capacity summed) */
+    uint64_t key_bytes;            /* bytes of packed CTF keys (h_keys[offset]) */
+    uint32_t oversize_kv_count;    /* oversize_buffer::oversize_kv_count */
+    uint32_t oversize_start_time_min, oversize_start_time_max;
+    uint32_t oversize_end_time_min, oversize_end_time_max;
+    uint32_t sid_count;            /* objects with keys in this window */
+    uint32_t oversize_oid_count;
+    uint32_t end_time_min;         /* base of the keys' end offsets */
+    uint32_t cur_time;             /* step time of the flush (end_time_max) */
+    uint32_t reserved;
+    uint64_t bits_outside;         /* bitmap bits beyond the bitmap array (dropped) */
+} glint_store_info;
+
+/* Flush now: the pending keys become the store (kept on the device until the
+ * next flush) and a new window starts at the last step's time.  Returns
+ * GLINT_ERR_UNSUPPORTED (GLINT_EF_STORE_DOMAIN) where the reference's own
+ * flush leaves its domain: a CTF without keys (its get_ctf_bits asserts),
+ * or CTF capacities that do not add up to the key count (meetings longer
+ * than max_meet_time shift the reference's CTF ranges). */
+glint_status glint_flush(glint_ctx *ctx, glint_store_info *info);
+/* The last flush's store, into host arrays (any may be NULL): keys
+ * (info.key_bytes), sids (num_objects u16, workbench::h_sids), ctf_capacity
+ * and ctfs (CTF_count each), bitmaps (CTF_count * 8192 bytes), the oversize
+ * buffer's keys (16-byte little-endian), boxes (4 floats each) and bitmap
+ * (8192 bytes). */
+glint_status glint_store_read(glint_ctx *ctx, uint8_t *keys, uint16_t *sids, uint32_t *ctf_capacity,
+                              glint_ctf_meta *ctfs, uint8_t *bitmaps, void *oversize_keys, float *oversize_boxes,
+                              uint8_t *oversize_bitmap, glint_store_info *info);
 
 /* ---- active contact search --------------------------------------------
  * search_info_unit (tracing/workbench.h:85-88): one active meeting of a

@@ -79,6 +79,36 @@ SEARCH_DTYPE = np.dtype([("pid", "<u4"), ("target", "<u4"), ("start", "<u4"), ("
 assert SEARCH_DTYPE.itemsize == 32
 
 
+# go_ctf_meta / glint_ctf_meta: CTF (tracing/step_merge.h) without its pointers
+CTF_META_DTYPE = np.dtype([("ctf_mbr", "<f4", (4,)), ("CTF_kv_capacity", "<u4"), ("start_time_min", "<u4"),
+                           ("start_time_max", "<u4"), ("end_time_min", "<u4"), ("end_time_max", "<u4"),
+                           ("ctf_bitmap_size", "<u4"), ("key_bit", "<u2"), ("id_bit", "<u2"),
+                           ("duration_bit", "<u2"), ("end_bit", "<u2"), ("low_x_bit", "<u2"), ("low_y_bit", "<u2"),
+                           ("edge_bit", "<u2"), ("mbr_bit", "<u2"), ("x_grid", "<u2"), ("y_grid", "<u2"),
+                           ("reserved", "<u4")])
+assert CTF_META_DTYPE.itemsize == 64
+BIT_BYTES = 256 * 256 // 8
+
+
+class GoStoreConfig(ctypes.Structure):
+    _fields_ = [("num_objects", ctypes.c_uint32), ("max_meet_time", ctypes.c_uint32), ("CTF_count", ctypes.c_uint32),
+                ("split_num", ctypes.c_uint32), ("first_end_time_min", ctypes.c_uint32), ("pad0", ctypes.c_uint32),
+                ("dProbFalse", ctypes.c_double), ("mbr", ctypes.c_double * 4), ("kv_capacity", ctypes.c_uint64)]
+
+
+class StoreInfo(ctypes.Structure):
+    """go_store_info / glint_store_info"""
+    _fields_ = [("kv_count", ctypes.c_uint64), ("key_bytes", ctypes.c_uint64), ("oversize_kv_count", ctypes.c_uint32),
+                ("oversize_start_time_min", ctypes.c_uint32), ("oversize_start_time_max", ctypes.c_uint32),
+                ("oversize_end_time_min", ctypes.c_uint32), ("oversize_end_time_max", ctypes.c_uint32),
+                ("sid_count", ctypes.c_uint32), ("oversize_oid_count", ctypes.c_uint32),
+                ("end_time_min", ctypes.c_uint32), ("cur_time", ctypes.c_uint32), ("reserved", ctypes.c_uint32),
+                ("bits_outside", ctypes.c_uint64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 def _load_oracle():
     build_oracle()  # make: a no-op unless a source is newer than the library
     lib = ctypes.CDLL(ORACLE_SO)
@@ -94,6 +124,17 @@ def _load_oracle():
     lib.go_get_buckets.argtypes = [vp, vp, vp, vp, vp]
     lib.go_active_search.restype = ctypes.c_uint64
     lib.go_active_search.argtypes = [vp, vp, ctypes.c_uint32, vp, ctypes.c_uint64]
+    lib.go_store_create.restype = vp
+    lib.go_store_create.argtypes = [ctypes.POINTER(GoStoreConfig)]
+    lib.go_store_destroy.argtypes = [vp]
+    lib.go_store_add_meetings.argtypes = [vp, vp, ctypes.c_uint64]
+    lib.go_store_kv_count.restype = ctypes.c_uint64
+    lib.go_store_kv_count.argtypes = [vp]
+    lib.go_store_flush.restype = ctypes.c_int
+    lib.go_store_flush.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(StoreInfo)]
+    lib.go_store_result.argtypes = [vp] * 9
+    lib.go_store_sorted.restype = ctypes.c_uint64
+    lib.go_store_sorted.argtypes = [vp, vp, vp]
     lib.go_dpm_lon.restype = ctypes.c_double
     lib.go_dpm_lon.argtypes = [ctypes.c_double]
     lib.go_sin_cr.restype = ctypes.c_double
@@ -184,6 +225,65 @@ class Oracle:
             pass
 
 
+class Store:
+    """CPU restatement of the GPU path's key generation and flush
+    (glint_flush_oracle.c)."""
+
+    def __init__(self, num_objects, mbr, *, max_meet_time=4096, CTF_count=100, split_num=10, first_end_time_min=5,
+                 dProbFalse=100.0, kv_capacity=1 << 22):
+        self.lib = oracle_lib()
+        self.cfg = GoStoreConfig(num_objects, max_meet_time, CTF_count, split_num, first_end_time_min, 0,
+                                 float(dProbFalse), (ctypes.c_double * 4)(*[float(v) for v in mbr]), int(kv_capacity))
+        self.h = self.lib.go_store_create(ctypes.byref(self.cfg))
+
+    def add_meetings(self, meetings: np.ndarray):
+        """meetings: records (pid1, pid2, start, end, mbr[4]) of one step"""
+        m = np.ascontiguousarray(meetings)
+        assert m.dtype.itemsize == 32
+        self.lib.go_store_add_meetings(self.h, m.ctypes.data, m.shape[0])
+
+    @property
+    def kv_count(self) -> int:
+        return int(self.lib.go_store_kv_count(self.h))
+
+    def flush(self, cur_time: int):
+        info = StoreInfo()
+        rc = self.lib.go_store_flush(self.h, int(cur_time), ctypes.byref(info))
+        return rc, info
+
+    def result(self, info: StoreInfo) -> dict:
+        C, N = self.cfg.CTF_count, self.cfg.num_objects
+        out = {"keys": np.zeros(int(info.key_bytes), np.uint8), "sids": np.zeros(N, np.uint16),
+               "ctf_capacity": np.zeros(C, np.uint32), "ctfs": np.zeros(C, CTF_META_DTYPE),
+               "bitmaps": np.zeros(C * BIT_BYTES, np.uint8),
+               "o_keys": np.zeros((int(info.oversize_kv_count), 16), np.uint8),
+               "o_boxes": np.zeros((int(info.oversize_kv_count), 4), np.float32),
+               "o_bitmap": np.zeros(BIT_BYTES, np.uint8)}
+        self.lib.go_store_result(self.h, *[out[k].ctypes.data for k in
+                                           ("keys", "sids", "ctf_capacity", "ctfs", "bitmaps", "o_keys", "o_boxes",
+                                            "o_bitmap")])
+        return out
+
+    def sorted_keys(self, info: StoreInfo):
+        """(keys as (n, 16) little-endian bytes, boxes (n, 4)) of the last flush"""
+        n = int(info.kv_count) + int(info.oversize_kv_count)
+        k = np.zeros((n, 16), np.uint8)
+        b = np.zeros((n, 4), np.float32)
+        self.lib.go_store_sorted(self.h, k.ctypes.data, b.ctypes.data)
+        return k, b
+
+    def close(self):
+        if self.h:
+            self.lib.go_store_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class RefConfig(ctypes.Structure):
     _fields_ = [
         ("num_objects", ctypes.c_uint32), ("num_threads", ctypes.c_uint32), ("grid_capacity", ctypes.c_uint32),
@@ -216,7 +316,8 @@ def ref_available() -> bool:
 def ref_lib():
     global _REF
     if _REF is None:
-        if not os.path.exists(REF_SO):
+        driver = os.path.join(HERE, "ref_driver.cpp")
+        if not os.path.exists(REF_SO) or os.path.getmtime(driver) > os.path.getmtime(REF_SO):
             if build_ref() is None:
                 raise FileNotFoundError("reference build unavailable (no sources on this machine)")
         lib = ctypes.CDLL(REF_SO)
@@ -233,6 +334,13 @@ def ref_lib():
         lib.ref_dpm_lon.restype = ctypes.c_double
         lib.ref_dpm_lon.argtypes = [ctypes.c_double]
         lib.ref_destroy.argtypes = [vp]
+        lib.ref_ctf_bits.argtypes = [vp, vp, ctypes.c_uint32, ctypes.c_uint32, vp, vp]
+        lib.ref_serial_mbr.restype = ctypes.c_uint64
+        lib.ref_serial_mbr.argtypes = [vp, vp, vp]
+        lib.ref_serial_key.argtypes = [vp, vp, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+                                       ctypes.c_uint64, vp]
+        lib.ref_ctf_find.restype = ctypes.c_int
+        lib.ref_ctf_find.argtypes = [vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
         _REF = lib
     return _REF
 

@@ -115,6 +115,66 @@ typedef struct go_search_info {
 uint64_t go_active_search(const go_ctx *c, const uint32_t *pids, uint32_t npids, go_search_info *out,
                           uint64_t cap);
 
+/* ---- key generation and flush into the key-value + bitmap store
+ * (glint_flush_oracle.c; cuda/geometry.cu:665-734, 739-1107, 1752-2135,
+ * tracing/step_merge.cpp:132-186) ---- */
+typedef struct go_store_config {
+    uint32_t num_objects;
+    uint32_t max_meet_time;       /* configuration::max_meet_time (4096) */
+    uint32_t CTF_count;           /* configuration::CTF_count (100) */
+    uint32_t split_num;           /* configuration::split_num (10) */
+    uint32_t first_end_time_min;  /* start_time + min_meet_time (tracing/process.cpp:404) */
+    uint32_t pad0;
+    double dProbFalse;            /* per-object area cut (tracing/process.cpp:408-411) */
+    double mbr[4];                /* map box: low x, low y, high x, high y */
+    uint64_t kv_capacity;         /* key buffer size */
+} go_store_config;
+
+/* one reported meeting, pid1 < pid2 */
+typedef struct go_meeting_rec {
+    uint32_t pid1, pid2, start, end;
+    float mbr[4];
+} go_meeting_rec;
+
+/* CTF (tracing/step_merge.h) without its pointers, 64 bytes */
+typedef struct go_ctf_meta {
+    float ctf_mbr[4];
+    uint32_t CTF_kv_capacity;
+    uint32_t start_time_min, start_time_max, end_time_min, end_time_max;
+    uint32_t ctf_bitmap_size;
+    uint16_t key_bit, id_bit, duration_bit, end_bit, low_x_bit, low_y_bit, edge_bit, mbr_bit, x_grid, y_grid;
+    uint32_t reserved;
+} go_ctf_meta;
+
+typedef struct go_store_info {
+    uint64_t kv_count;            /* keys in the CTFs */
+    uint64_t key_bytes;           /* bytes of packed CTF keys */
+    uint32_t oversize_kv_count;
+    uint32_t oversize_start_time_min, oversize_start_time_max;
+    uint32_t oversize_end_time_min, oversize_end_time_max;
+    uint32_t sid_count;
+    uint32_t oversize_oid_count;
+    uint32_t end_time_min;        /* the window's base for key end offsets */
+    uint32_t cur_time;
+    uint32_t reserved;
+    uint64_t bits_outside;        /* bitmap bits past the end of the bitmap array (dropped) */
+} go_store_info;
+
+typedef struct go_store go_store;
+go_store *go_store_create(const go_store_config *cfg);
+void go_store_destroy(go_store *s);
+void go_store_add_meetings(go_store *s, const go_meeting_rec *m, uint64_t n);
+uint64_t go_store_kv_count(const go_store *s);
+/* 0 on success; <0 outside the reference's domain (an empty CTF, key overflow) */
+int go_store_flush(go_store *s, uint32_t cur_time, go_store_info *out);
+/* the last flush's outputs; o_keys are 16-byte little-endian keys */
+void go_store_result(const go_store *s, uint8_t *keys, uint16_t *sids, uint32_t *ctf_capacity, go_ctf_meta *ctfs,
+                     uint8_t *bitmaps, void *o_keys, float *o_boxes, uint8_t *o_bitmap);
+
+/* the last flush's sorted 16-byte keys (CTF part, then oversize part) and
+ * boxes; returns their number */
+uint64_t go_store_sorted(const go_store *s, void *keys, float *boxes);
+
 /* correctly rounded sin on [0, pi/2] by a double-double Taylor series; used to
  * check how often libm's sin differs from the correctly rounded value */
 double go_sin_cr(double x);

@@ -199,4 +199,82 @@ void ref_destroy(void *hv) {
     delete h;
 }
 
+/* ---- the reference's own CTF encoding (tracing/step_merge.cpp), used to pin
+ * the flush restatement's bit widths, box quantisation and key layout ---- */
+
+/* CTF::get_ctf_bits for a CTF box; bits = key_bit, id_bit, duration_bit,
+ * end_bit, low_x_bit, low_y_bit, edge_bit, mbr_bit, x_grid, y_grid */
+void ref_ctf_bits(const float *ctf_mbr4, const double *map4, uint32_t num_objects, uint32_t max_meet_time,
+                  uint16_t *bits, uint32_t *bitmap_size) {
+    CTF c;
+    c.ctf_mbr.low[0] = ctf_mbr4[0];
+    c.ctf_mbr.low[1] = ctf_mbr4[1];
+    c.ctf_mbr.high[0] = ctf_mbr4[2];
+    c.ctf_mbr.high[1] = ctf_mbr4[3];
+    box map(map4[0], map4[1], map4[2], map4[3]);
+    configuration cfg;
+    cfg.num_objects = num_objects;
+    cfg.max_meet_time = max_meet_time;
+    c.get_ctf_bits(map, &cfg);
+    bits[0] = c.key_bit; bits[1] = c.id_bit; bits[2] = c.duration_bit; bits[3] = c.end_bit;
+    bits[4] = c.low_x_bit; bits[5] = c.low_y_bit; bits[6] = c.edge_bit; bits[7] = c.mbr_bit;
+    bits[8] = c.x_grid; bits[9] = c.y_grid;
+    *bitmap_size = c.ctf_bitmap_size;
+}
+
+static void ref_ctf_from(CTF &c, const float *ctf_mbr4, const uint16_t *bits) {
+    c.ctf_mbr.low[0] = ctf_mbr4[0];
+    c.ctf_mbr.low[1] = ctf_mbr4[1];
+    c.ctf_mbr.high[0] = ctf_mbr4[2];
+    c.ctf_mbr.high[1] = ctf_mbr4[3];
+    c.key_bit = bits[0]; c.id_bit = bits[1]; c.duration_bit = bits[2]; c.end_bit = bits[3];
+    c.low_x_bit = bits[4]; c.low_y_bit = bits[5]; c.edge_bit = bits[6]; c.mbr_bit = bits[7];
+    c.x_grid = bits[8]; c.y_grid = bits[9];
+}
+
+/* CTF::serial_mbr of a box inside the CTF box */
+uint64_t ref_serial_mbr(const float *ctf_mbr4, const uint16_t *bits, const float *box4) {
+    CTF c;
+    ref_ctf_from(c, ctf_mbr4, bits);
+    f_box b;
+    b.low[0] = box4[0];
+    b.low[1] = box4[1];
+    b.high[0] = box4[2];
+    b.high[1] = box4[3];
+    return c.serial_mbr(&b);
+}
+
+/* CTF::serial_key, as 16 little-endian bytes */
+void ref_serial_key(const float *ctf_mbr4, const uint16_t *bits, uint64_t pid, uint64_t target, uint64_t duration,
+                    uint64_t end, uint64_t value_mbr, uint8_t *out16) {
+    CTF c;
+    ref_ctf_from(c, ctf_mbr4, bits);
+    __uint128_t k = c.serial_key(pid, target, duration, end, (__uint128_t)value_mbr);
+    std::memcpy(out16, &k, 16);
+}
+
+/* CTF::binary_search + the key walk of search_SSTable over packed keys:
+ * the first index holding oid and the number of consecutive keys of oid */
+int ref_ctf_find(const float *ctf_mbr4, const uint16_t *bits, const uint8_t *keys, uint32_t n, uint32_t oid,
+                 uint32_t *count) {
+    CTF c;
+    ref_ctf_from(c, ctf_mbr4, bits);
+    c.CTF_kv_capacity = n;
+    c.keys = reinterpret_cast<__uint128_t *>(const_cast<uint8_t *>(keys));
+    const int find = c.binary_search(oid);
+    uint32_t k = 0;
+    if (find >= 0) {
+        __uint128_t t = 0;
+        for (uint32_t i = (uint32_t)find; i < n; ++i) {
+            t = 0;
+            std::memcpy(&t, keys + (size_t)i * c.key_bit / 8, c.key_bit / 8);
+            if (c.ctf_get_key_oid(t) != oid) break;
+            ++k;
+        }
+    }
+    *count = k;
+    c.keys = nullptr;
+    return find;
+}
+
 } /* extern "C" */
