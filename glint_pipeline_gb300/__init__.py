@@ -60,6 +60,7 @@ class Configuration:
     timing: bool = False
     auto_flush: bool = False
     split_num: int = 10
+    store_keep: int = 16                # flushed blocks kept on the device for queries
     kv_restriction: int = 0             # 0 -> G_bytes * 2^25 keys (config.h:80)
     kv_capacity: int = 0                # 0 -> kv_restriction + 1000000 (config.h:81)
 
@@ -194,6 +195,40 @@ class DeviceBench:
             raise GlintError(st, self.last_error())
         out["info"] = info
         return out
+
+    def store_blocks(self) -> int:
+        return int(self.lib.glint_store_blocks(self.h))
+
+    def query(self, queries):
+        """Contact-trace queries over the kept store blocks.  queries: a list of
+        (seeds, hops, t_start, t_end); returns, per query, a list of per-hop
+        arrays of newly reached object ids (ascending), and the keys scanned."""
+        n = len(queries)
+        qs = (_abi.GlintQuery * max(n, 1))()
+        rs = (_abi.GlintQueryResult * max(n, 1))()
+        keep = []
+        for i, (seeds, hops, t0, t1) in enumerate(queries):
+            sd = np.ascontiguousarray(seeds, dtype=np.uint32)
+            keep.append(sd)
+            qs[i].seeds = sd.ctypes.data_as(ctypes.c_void_p).value if sd.size else None
+            qs[i].n_seeds, qs[i].hops, qs[i].t_start, qs[i].t_end = sd.size, int(hops), int(t0), int(t1)
+            rs[i].ids, rs[i].cap = None, 0
+        st = self.lib.glint_query_batch(self.h, qs, n, rs)
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        bufs = []
+        for i in range(n):
+            b = np.zeros(max(int(rs[i].n), 1), np.uint32)
+            bufs.append(b)
+            rs[i].ids, rs[i].cap = b.ctypes.data_as(ctypes.c_void_p).value, b.size
+        st = self.lib.glint_query_batch(self.h, qs, n, rs)
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        out = []
+        for i, (seeds, hops, t0, t1) in enumerate(queries):
+            ends = [0] + [int(rs[i].hop_end[h]) for h in range(int(hops))]
+            out.append([bufs[i][ends[h]:ends[h + 1]] for h in range(int(hops))])
+        return out, int(rs[0].keys_scanned) if n else 0
 
     # -- state ------------------------------------------------------------------
     def schema(self):

@@ -50,7 +50,7 @@ class GlintConfig(ctypes.Structure):
         ("timing", ctypes.c_uint32),
         ("auto_flush", ctypes.c_uint32),
         ("split_num", ctypes.c_uint32),
-        ("reserved0", ctypes.c_uint32),
+        ("store_keep", ctypes.c_uint32),
         ("kv_restriction", ctypes.c_uint64),
         ("kv_capacity", ctypes.c_uint64),
     ]
@@ -137,6 +137,16 @@ class GlintStoreInfo(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
 
 
+class GlintQuery(ctypes.Structure):
+    _fields_ = [("seeds", ctypes.c_void_p), ("n_seeds", ctypes.c_uint32), ("hops", ctypes.c_uint32),
+                ("t_start", ctypes.c_uint32), ("t_end", ctypes.c_uint32)]
+
+
+class GlintQueryResult(ctypes.Structure):
+    _fields_ = [("ids", ctypes.c_void_p), ("cap", ctypes.c_uint64), ("n", ctypes.c_uint64),
+                ("hop_end", ctypes.c_uint64 * 8), ("keys_scanned", ctypes.c_uint64)]
+
+
 # glint_search_info = search_info_unit (tracing/workbench.h:85-88)
 SEARCH_DTYPE = np.dtype([("pid", "<u4"), ("target", "<u4"), ("start", "<u4"), ("end", "<u4"), ("mbr", "<f4", (4,))])
 assert SEARCH_DTYPE.itemsize == 32
@@ -171,6 +181,9 @@ def load_library(path: str | None = None):
     lib.glint_stream.argtypes = [vp]
     lib.glint_active_search.argtypes = [vp, vp, u32, vp, u64, ctypes.POINTER(u64)]
     lib.glint_flush.argtypes = [vp, ctypes.POINTER(GlintStoreInfo)]
+    lib.glint_query_batch.argtypes = [vp, ctypes.POINTER(GlintQuery), u32, ctypes.POINTER(GlintQueryResult)]
+    lib.glint_store_blocks.restype = u32
+    lib.glint_store_blocks.argtypes = [vp]
     lib.glint_store_read.argtypes = [vp] * 9 + [ctypes.POINTER(GlintStoreInfo)]
     lib.glint_active_search_noalloc.argtypes = [vp, vp, u32, vp, u64, vp]
     lib.glint_gen_create.argtypes = [vp, u32, vp, u32, u32, u32, ctypes.POINTER(vp)]

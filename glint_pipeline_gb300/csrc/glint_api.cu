@@ -179,6 +179,8 @@ void free_all(glint_ctx *c) {
     for (void *p : ptrs)
         if (p) cudaFree(p);
     flush_free(c);
+    store_blocks_free(c);
+    query_pool_free(c);
     if (c->h_cnt) cudaFreeHost(c->h_cnt);
     if (c->timers.created) {
         for (auto &e : c->timers.ev) cudaEventDestroy(e);
@@ -277,6 +279,7 @@ void glint_config_defaults(glint_config *cfg, uint32_t n) {
     cfg->dProbFalse = 100;
     cfg->precision_mode = 0;
     cfg->split_num = 10;
+    cfg->store_keep = 16;
 }
 
 glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, const double *first_points,

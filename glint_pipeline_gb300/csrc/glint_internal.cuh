@@ -78,6 +78,45 @@ struct SchemaEvent {
     uint32_t kind;        /* 0 split, 1 merge */
 };
 
+/* one flushed contact-tracing block (CTB) kept on the device for queries */
+struct StoreBlock {
+    uint8_t *keys = nullptr;               /* packed CTF keys */
+    uint64_t key_bytes = 0;
+    glint_ctf_meta *ctfs = nullptr;        /* [C] */
+    unsigned long long *key_index = nullptr, *byte_index = nullptr; /* [C] */
+    uint16_t *sids = nullptr;              /* [N] 0 none, 1 oversize, 2.. CTF + 2 */
+    uint32_t *first = nullptr, *count = nullptr; /* [N] each object's keys (in its CTF or the oversize buffer) */
+    ulonglong2 *okeys = nullptr;           /* oversize keys, 128-bit */
+    uint64_t kv = 0, o_count = 0;
+    uint32_t end_time_min = 0, end_time_max = 0;
+};
+
+/* device-side descriptor of a StoreBlock */
+struct StoreBlockDev {
+    const uint8_t *keys;
+    const glint_ctf_meta *ctfs;
+    const unsigned long long *key_index, *byte_index;
+    const uint16_t *sids;
+    const uint32_t *first, *count;
+    const ulonglong2 *okeys;
+    uint32_t end_time_min;
+    uint32_t C;
+};
+
+/* per-query scratch of glint_query_batch, grown on demand */
+struct QueryPool {
+    uint32_t slots = 0;
+    uint32_t *visited = nullptr;           /* [slots][words] */
+    uint32_t *lists = nullptr;             /* [slots][2][N] frontier / next */
+    uint32_t *counts = nullptr;            /* [slots] next counts */
+    uint32_t *seeds = nullptr;
+    uint64_t seeds_cap = 0;
+    unsigned long long *prefix = nullptr;  /* [slots + 1] */
+    uint32_t *qparam = nullptr;            /* [slots][4] t_start, t_end, window, cur list */
+    StoreBlockDev *blocks = nullptr;
+    uint32_t blocks_cap = 0;
+};
+
 struct StepTimers {
     cudaEvent_t ev[9];
     bool created = false;
@@ -176,6 +215,8 @@ struct glint_ctx {
     float4 *store_boxes_ptr = nullptr;
     uint64_t store_kv = 0;
     uint32_t flushes = 0;
+    std::vector<glint::StoreBlock> ctbs;   /* flushed blocks kept for queries, oldest first */
+    glint::QueryPool qpool;
     cudaEvent_t flush_ev[2];
     float last_flush_ms = 0;
     bool last_flushed = false;
@@ -219,6 +260,8 @@ cudaError_t flush_alloc(glint_ctx *c);
 void flush_free(glint_ctx *c);
 void flush_set_attributes();
 glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err);
+void store_blocks_free(glint_ctx *c);
+void query_pool_free(glint_ctx *c);
 
 inline ExactCtx make_exact(glint_ctx *c) {
     ExactCtx e;

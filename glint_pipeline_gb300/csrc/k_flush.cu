@@ -555,6 +555,18 @@ __global__ void k_ctf_pack(const u128 *__restrict__ keys, const float4 *__restri
     }
 }
 
+/* where each object's keys sit in a flushed block: its CTF part index or its
+ * oversize-buffer index, and how many */
+__global__ void k_block_index(uint32_t N, const uint32_t *__restrict__ seg_of, const uint32_t *__restrict__ same,
+                              const uint8_t *__restrict__ over, uint64_t kv, uint32_t *__restrict__ first,
+                              uint32_t *__restrict__ count) {
+    for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < N; id += gridDim.x * blockDim.x) {
+        const uint32_t n = same[id];
+        count[id] = n;
+        first[id] = n ? (over[id] ? (uint32_t)(seg_of[id] - kv) : seg_of[id]) : 0u;
+    }
+}
+
 /* CTF::get_ctf_bits + eight_parallel (tracing/step_merge.cpp:132-186) on the
  * host, in the reference's double arithmetic; false where its asserts fire */
 uint32_t min_bits_to_store(uint32_t v) {
@@ -853,6 +865,52 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
     c->store_valid = true;
     if (info) *info = inf;
 
+    /* keep the block on the device for queries */
+    if (c->cfg.store_keep) {
+        StoreBlock b;
+        const size_t bytes_keys = bytes ? bytes : 1;
+        cudaError_t ae = cudaSuccess;
+        auto A = [&](void **p, size_t n) {
+            if (ae == cudaSuccess) ae = cudaMalloc(p, n ? n : 1);
+        };
+        A((void **)&b.keys, bytes_keys);
+        A((void **)&b.ctfs, sizeof(glint_ctf_meta) * C);
+        A((void **)&b.key_index, sizeof(unsigned long long) * C);
+        A((void **)&b.byte_index, sizeof(unsigned long long) * C);
+        A((void **)&b.sids, sizeof(uint16_t) * N);
+        A((void **)&b.first, sizeof(uint32_t) * N);
+        A((void **)&b.count, sizeof(uint32_t) * N);
+        A((void **)&b.okeys, sizeof(ulonglong2) * o_n);
+        if (ae != cudaSuccess) {
+            void *ps[] = {b.keys, b.ctfs, b.key_index, b.byte_index, b.sids, b.first, b.count, b.okeys};
+            for (void *p : ps)
+                if (p) cudaFree(p);
+            return fail(ae, "keep block");
+        }
+        if (bytes) cudaMemcpyAsync(b.keys, c->d_ctf_keys, bytes, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(b.ctfs, c->d_ctfs, sizeof(glint_ctf_meta) * C, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(b.key_index, c->d_ctf_lo, sizeof(unsigned long long) * C, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(b.byte_index, c->d_ctf_byte, sizeof(unsigned long long) * C, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(b.sids, c->d_sids, sizeof(uint16_t) * N, cudaMemcpyDeviceToDevice, s);
+        if (o_n)
+            cudaMemcpyAsync(b.okeys, c->d_keys + kv, sizeof(ulonglong2) * o_n, cudaMemcpyDeviceToDevice, s);
+        k_block_index<<<grid_for(N, 256), 256, 0, s>>>(N, c->d_segof, c->d_same, c->d_over, kv, b.first, b.count);
+        b.kv = kv;
+        b.o_count = o_n;
+        b.key_bytes = bytes;
+        b.end_time_min = c->end_time_min;
+        b.end_time_max = c->last_time;
+        c->ctbs.push_back(b);
+        while (c->ctbs.size() > c->cfg.store_keep) {
+            StoreBlock &o = c->ctbs.front();
+            cudaStreamSynchronize(s);
+            void *ps[] = {o.keys, o.ctfs, o.key_index, o.byte_index, o.sids, o.first, o.count, o.okeys};
+            for (void *p : ps)
+                if (p) cudaFree(p);
+            c->ctbs.erase(c->ctbs.begin());
+        }
+    }
+
     /* the next window (cuda/geometry.cu:2112-2131, tracing/process.cpp:271,549);
      * the sids array is kept as the store's and cleared at the next key */
     cudaMemcpyAsync(c->d_sids_out, c->d_sids, sizeof(uint16_t) * N, cudaMemcpyDeviceToDevice, s);
@@ -927,3 +985,14 @@ extern "C" glint_status glint_store_read(glint_ctx *c, uint8_t *keys, uint16_t *
     if (info) *info = inf;
     return GLINT_OK;
 }
+
+namespace glint {
+void store_blocks_free(glint_ctx *c) {
+    for (StoreBlock &o : c->ctbs) {
+        void *ps[] = {o.keys, o.ctfs, o.key_index, o.byte_index, o.sids, o.first, o.count, o.okeys};
+        for (void *p : ps)
+            if (p) cudaFree(p);
+    }
+    c->ctbs.clear();
+}
+} // namespace glint

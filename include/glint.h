@@ -17,7 +17,7 @@
  * returned by glint_meetings().  The flush of finished meetings into the
  * sorted key-value + bitmap store (cuda/geometry.cu:1752-2135,
  * tracing/step_merge.cpp:132-186) is glint_flush(); contact-trace queries
- * against that store are glint_query_*().
+ * against that store are glint_query_batch().
  *
  * Plain pointers and sizes only.  Every call returns a status instead of
  * exiting (the reference's CUDA_SAFE_CALL exits, cuda/cuda_util.cuh:19-27).
@@ -90,7 +90,8 @@ typedef struct glint_config {
     uint32_t auto_flush;           /* 1: flush inside the step once more than kv_restriction keys are
                                       pending, as cuda/geometry.cu:1752 */
     uint32_t split_num;            /* configuration::split_num (10): STR slices per axis */
-    uint32_t reserved0;
+    uint32_t store_keep;           /* flushed blocks (CTBs) kept on the device for glint_query_batch;
+                                      0 -> none; the oldest is dropped first */
     uint64_t kv_restriction;       /* 0 -> G_bytes*2^25 keys (util/config.h:80) */
     uint64_t kv_capacity;          /* key buffer; 0 -> kv_restriction + 1000000 (util/config.h:81) */
 } glint_config;
@@ -259,6 +260,38 @@ glint_status glint_flush(glint_ctx *ctx, glint_store_info *info);
 glint_status glint_store_read(glint_ctx *ctx, uint8_t *keys, uint16_t *sids, uint32_t *ctf_capacity,
                               glint_ctf_meta *ctfs, uint8_t *bitmaps, void *oversize_keys, float *oversize_boxes,
                               uint8_t *oversize_bitmap, glint_store_info *info);
+
+/* ---- contact-trace queries over the flushed store ---------------------------
+ * The reference reads its store per object (id_search_in_CTB,
+ * tracing/workbench.cpp:397-444): the object's sid picks its CTF or the
+ * oversize buffer, CTF::binary_search / oversize_buffer::search_buffer find
+ * its keys (tracing/step_merge.cpp:67-115, 501-568), and the targets found
+ * seed the next hop (search_multi_pid, tracing/process.cpp:476-495).  Here a
+ * batch of queries runs on the device over the blocks kept by
+ * glint_config.store_keep: hop h+1 expands every object first reached at
+ * hop h; a key (pid, target, duration, end) counts when its meeting
+ * [end - duration, end] overlaps [t_start, t_end) (start < t_end &&
+ * t_start < end; both 0: no window, the reference's abandon = true). */
+typedef struct glint_query {
+    const uint32_t *seeds;         /* host array */
+    uint32_t n_seeds;
+    uint32_t hops;                 /* 1..8 */
+    uint32_t t_start, t_end;
+} glint_query;
+
+typedef struct glint_query_result {
+    uint32_t *ids;                 /* host array for the reached objects, or NULL */
+    uint64_t cap;                  /* its length */
+    uint64_t n;                    /* out: objects reached over all hops (seeds excluded) */
+    uint64_t hop_end[8];           /* out: ids[hop_end[h-1] .. hop_end[h]) were first reached at hop h,
+                                      each hop's ids ascending */
+    uint64_t keys_scanned;         /* out: keys read */
+} glint_query_result;
+
+glint_status glint_query_batch(glint_ctx *ctx, const glint_query *queries, uint32_t num_queries,
+                               glint_query_result *results);
+/* number of flushed blocks currently kept for queries */
+uint32_t glint_store_blocks(const glint_ctx *ctx);
 
 /* ---- active contact search --------------------------------------------
  * search_info_unit (tracing/workbench.h:85-88): one active meeting of a

@@ -135,6 +135,9 @@ def _load_oracle():
     lib.go_store_result.argtypes = [vp] * 9
     lib.go_store_sorted.restype = ctypes.c_uint64
     lib.go_store_sorted.argtypes = [vp, vp, vp]
+    lib.go_query_bfs.restype = ctypes.c_uint64
+    lib.go_query_bfs.argtypes = [vp, ctypes.c_uint64, ctypes.c_uint32, vp, ctypes.c_uint32, ctypes.c_uint32,
+                                 ctypes.c_uint32, ctypes.c_uint32, vp, ctypes.c_uint64, vp]
     lib.go_dpm_lon.restype = ctypes.c_double
     lib.go_dpm_lon.argtypes = [ctypes.c_double]
     lib.go_sin_cr.restype = ctypes.c_double
@@ -223,6 +226,25 @@ class Oracle:
             self.close()
         except Exception:
             pass
+
+
+EDGE_DTYPE = np.dtype([("pid", "<u4"), ("target", "<u4"), ("start", "<u4"), ("end", "<u4")])
+
+
+def query_bfs(edges: np.ndarray, num_objects: int, seeds, hops: int, t_start: int = 0, t_end: int = 0):
+    """Contact-trace BFS over store edges (glint_query_oracle.c): a list of
+    per-hop arrays of newly reached object ids (ascending)."""
+    lib = oracle_lib()
+    e = np.ascontiguousarray(edges, dtype=EDGE_DTYPE)
+    sd = np.ascontiguousarray(seeds, dtype=np.uint32)
+    hop_end = np.zeros(max(hops, 1), np.uint64)
+    n = lib.go_query_bfs(e.ctypes.data, e.shape[0], num_objects, sd.ctypes.data, sd.shape[0], t_start, t_end, hops,
+                         None, 0, hop_end.ctypes.data)
+    out = np.zeros(max(int(n), 1), np.uint32)
+    lib.go_query_bfs(e.ctypes.data, e.shape[0], num_objects, sd.ctypes.data, sd.shape[0], t_start, t_end, hops,
+                     out.ctypes.data, out.shape[0], hop_end.ctypes.data)
+    bounds = [0] + [int(v) for v in hop_end[:hops]]
+    return [out[bounds[h]:bounds[h + 1]] for h in range(hops)]
 
 
 class Store:

@@ -175,6 +175,20 @@ void go_store_result(const go_store *s, uint8_t *keys, uint16_t *sids, uint32_t 
  * boxes; returns their number */
 uint64_t go_store_sorted(const go_store *s, void *keys, float *boxes);
 
+/* ---- contact-trace queries over the store (glint_query_oracle.c) ---- */
+/* one key of the store as a meeting edge */
+typedef struct go_edge {
+    uint32_t pid, target, start, end;
+} go_edge;
+
+/* objects first reached at each of `hops` hops from the seeds over edges
+ * overlapping [t_start, t_end) (t_start == t_end == 0: no window), each hop's
+ * ids ascending, seeds excluded; hop_end[h] = ids after hop h; returns the
+ * total (only the first cap are written) */
+uint64_t go_query_bfs(const go_edge *edges, uint64_t n_edges, uint32_t num_objects, const uint32_t *seeds,
+                      uint32_t n_seeds, uint32_t t_start, uint32_t t_end, uint32_t hops, uint32_t *out,
+                      uint64_t cap, uint64_t *hop_end);
+
 /* correctly rounded sin on [0, pi/2] by a double-double Taylor series; used to
  * check how often libm's sin differs from the correctly rounded value */
 double go_sin_cr(double x);

@@ -1,0 +1,75 @@
+"""Contact-trace queries over the flushed store on the GPU against the
+oracle's breadth-first restatement over the same meetings."""
+import numpy as np
+import pytest
+
+from glint_pipeline_gb300 import Configuration, DeviceBench
+from oracle.bindings import EDGE_DTYPE, query_bfs
+from workloads import case_config, make_points
+
+pytestmark = pytest.mark.gpu
+
+
+def build_store(name, steps, flush_at, keep=16):
+    box, pts = make_points(name, steps)
+    cfgd = case_config(name)
+    c = Configuration(num_objects=cfgd["num_objects"], grid_capacity=cfgd["grid_capacity"],
+                      grid_amplify=cfgd["grid_amplify"], num_meeting_buckets=cfgd["num_meeting_buckets"],
+                      reach_distance=cfgd["reach_distance"], min_meet_time=cfgd["min_meet_time"],
+                      schema_update_delay=cfgd["schema_update_delay"], kv_capacity=1 << 22, store_keep=keep)
+    g = DeviceBench(c, box, pts[0])
+    windows = []   # meetings of each flushed window
+    cur = []
+    for t in range(steps):
+        g.step(pts[t], t)
+        cur.append(g.meetings())
+        if t in flush_at:
+            g.flush()
+            windows.append(np.concatenate(cur))
+            cur = []
+    return g, cfgd["num_objects"], windows
+
+
+def edges_of(meetings):
+    e = np.zeros(2 * len(meetings), EDGE_DTYPE)
+    e["pid"][0::2], e["target"][0::2] = meetings["pid1"], meetings["pid2"]
+    e["pid"][1::2], e["target"][1::2] = meetings["pid2"], meetings["pid1"]
+    e["start"][0::2] = e["start"][1::2] = meetings["start"]
+    e["end"][0::2] = e["end"][1::2] = meetings["end"]
+    return e
+
+
+def check(g, n, edges, queries):
+    got, scanned = g.query(queries)
+    assert scanned > 0
+    for (seeds, hops, t0, t1), res in zip(queries, got):
+        want = query_bfs(edges, n, seeds, hops, t0, t1)
+        for h in range(hops):
+            np.testing.assert_array_equal(res[h], want[h], err_msg=f"hop {h + 1} of {len(seeds)} seeds, {t0}-{t1}")
+
+
+def test_query_matches_oracle_bfs():
+    g, n, windows = build_store("dense_20k", 50, (20, 35, 49))
+    assert g.store_blocks() == 3
+    edges = edges_of(np.concatenate(windows))
+    rng = np.random.default_rng(3)
+    queries = []
+    for k, hops, win in [(1, 3, (0, 0)), (10, 2, (0, 0)), (100, 1, (0, 0)), (1000, 3, (0, 0)), (50, 3, (10, 30)),
+                         (200, 2, (0, 6)), (30, 3, (40, 50))]:
+        seeds = rng.choice(n, k, replace=False).astype(np.uint32)
+        queries.append((seeds, hops, win[0], win[1]))
+    queries.append((np.array([5, 5, 7, 10 ** 9], np.uint32), 2, 0, 0))  # repeats and an id past N
+    check(g, n, edges, queries)
+    # a batch larger than one chunk of query slots
+    big = [(rng.choice(n, 20, replace=False).astype(np.uint32), 2, 0, 0) for _ in range(70)]
+    check(g, n, edges, big)
+    g.close()
+
+
+def test_query_kept_blocks_only():
+    g, n, windows = build_store("dense_20k", 40, (12, 25, 39), keep=2)
+    assert g.store_blocks() == 2
+    edges = edges_of(np.concatenate(windows[1:]))
+    rng = np.random.default_rng(4)
+    check(g, n, edges, [(rng.choice(n, 300, replace=False).astype(np.uint32), 3, 0, 0)])
+    g.close()
