@@ -228,7 +228,7 @@ class DeviceBench:
         for i, (seeds, hops, t0, t1) in enumerate(queries):
             ends = [0] + [int(rs[i].hop_end[h]) for h in range(int(hops))]
             out.append([bufs[i][ends[h]:ends[h + 1]] for h in range(int(hops))])
-        return out, int(rs[0].keys_scanned) if n else 0
+        return out, sum(int(rs[i].keys_scanned) for i in range(n))
 
     # -- state ------------------------------------------------------------------
     def schema(self):
@@ -266,6 +266,67 @@ class DeviceBench:
     def close(self):
         if getattr(self, "h", None):
             self.lib.glint_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """Continuous-batching query server over a DeviceBench's kept store blocks
+    (glint_server_*)."""
+
+    def __init__(self, bench: DeviceBench, max_slots: int = 64):
+        self.bench = bench
+        self.lib = bench.lib
+        h = ctypes.c_void_p()
+        st = self.lib.glint_server_create(bench.h, int(max_slots), ctypes.byref(h))
+        if st != 0:
+            raise GlintError(st, bench.last_error())
+        self.h = h
+        self.slots = int(self.lib.glint_server_slots(h))
+        self._keep = {}
+
+    def submit(self, seeds, hops: int, t_start: int = 0, t_end: int = 0) -> int:
+        sd = np.ascontiguousarray(seeds, dtype=np.uint32)
+        q = _abi.GlintQuery()
+        q.seeds = sd.ctypes.data_as(ctypes.c_void_p).value if sd.size else None
+        q.n_seeds, q.hops, q.t_start, q.t_end = sd.size, int(hops), int(t_start), int(t_end)
+        t = ctypes.c_uint64()
+        st = self.lib.glint_server_submit(self.h, ctypes.byref(q), ctypes.byref(t))
+        if st != 0:
+            raise GlintError(st, self.bench.last_error())
+        self._keep[t.value] = int(hops)
+        return t.value
+
+    def step(self):
+        a, q = ctypes.c_uint32(), ctypes.c_uint32()
+        st = self.lib.glint_server_step(self.h, ctypes.byref(a), ctypes.byref(q))
+        if st != 0:
+            raise GlintError(st, self.bench.last_error())
+        return a.value, q.value
+
+    def poll(self, ticket: int, cap: int = 1 << 20):
+        """None while running; else (per-hop id arrays, keys scanned)"""
+        buf = np.zeros(max(cap, 1), np.uint32)
+        r = _abi.GlintQueryResult()
+        r.ids, r.cap = buf.ctypes.data_as(ctypes.c_void_p).value, buf.size
+        done = ctypes.c_int()
+        st = self.lib.glint_server_poll(self.h, int(ticket), ctypes.byref(r), ctypes.byref(done))
+        if st != 0:
+            raise GlintError(st, self.bench.last_error())
+        if not done.value:
+            return None
+        hops = self._keep.pop(int(ticket))
+        ends = [0] + [min(int(r.hop_end[h]), buf.size) for h in range(hops)]
+        return [buf[ends[h]:ends[h + 1]] for h in range(hops)], int(r.keys_scanned), int(r.n)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.glint_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

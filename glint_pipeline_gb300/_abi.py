@@ -184,6 +184,13 @@ def load_library(path: str | None = None):
     lib.glint_query_batch.argtypes = [vp, ctypes.POINTER(GlintQuery), u32, ctypes.POINTER(GlintQueryResult)]
     lib.glint_store_blocks.restype = u32
     lib.glint_store_blocks.argtypes = [vp]
+    lib.glint_server_create.argtypes = [vp, u32, ctypes.POINTER(vp)]
+    lib.glint_server_destroy.argtypes = [vp]
+    lib.glint_server_slots.restype = u32
+    lib.glint_server_slots.argtypes = [vp]
+    lib.glint_server_submit.argtypes = [vp, ctypes.POINTER(GlintQuery), ctypes.POINTER(u64)]
+    lib.glint_server_step.argtypes = [vp, ctypes.POINTER(u32), ctypes.POINTER(u32)]
+    lib.glint_server_poll.argtypes = [vp, u64, ctypes.POINTER(GlintQueryResult), ctypes.POINTER(ctypes.c_int)]
     lib.glint_store_read.argtypes = [vp] * 9 + [ctypes.POINTER(GlintStoreInfo)]
     lib.glint_active_search_noalloc.argtypes = [vp, vp, u32, vp, u64, vp]
     lib.glint_gen_create.argtypes = [vp, u32, vp, u32, u32, u32, ctypes.POINTER(vp)]

@@ -180,7 +180,8 @@ void free_all(glint_ctx *c) {
         if (p) cudaFree(p);
     flush_free(c);
     store_blocks_free(c);
-    query_pool_free(c);
+    server_free_default(c);
+    servers_detach(c);
     if (c->h_cnt) cudaFreeHost(c->h_cnt);
     if (c->timers.created) {
         for (auto &e : c->timers.ev) cudaEventDestroy(e);

@@ -103,20 +103,6 @@ struct StoreBlockDev {
     uint32_t C;
 };
 
-/* per-query scratch of glint_query_batch, grown on demand */
-struct QueryPool {
-    uint32_t slots = 0;
-    uint32_t *visited = nullptr;           /* [slots][words] */
-    uint32_t *lists = nullptr;             /* [slots][2][N] frontier / next */
-    uint32_t *counts = nullptr;            /* [slots] next counts */
-    uint32_t *seeds = nullptr;
-    uint64_t seeds_cap = 0;
-    unsigned long long *prefix = nullptr;  /* [slots + 1] */
-    uint32_t *qparam = nullptr;            /* [slots][4] t_start, t_end, window, cur list */
-    StoreBlockDev *blocks = nullptr;
-    uint32_t blocks_cap = 0;
-};
-
 struct StepTimers {
     cudaEvent_t ev[9];
     bool created = false;
@@ -216,7 +202,8 @@ struct glint_ctx {
     uint64_t store_kv = 0;
     uint32_t flushes = 0;
     std::vector<glint::StoreBlock> ctbs;   /* flushed blocks kept for queries, oldest first */
-    glint::QueryPool qpool;
+    glint_server *server = nullptr;        /* the default server behind glint_query_batch */
+    std::vector<glint_server *> servers;   /* every live server on this context */
     cudaEvent_t flush_ev[2];
     float last_flush_ms = 0;
     bool last_flushed = false;
@@ -261,7 +248,8 @@ void flush_free(glint_ctx *c);
 void flush_set_attributes();
 glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err);
 void store_blocks_free(glint_ctx *c);
-void query_pool_free(glint_ctx *c);
+void server_free_default(glint_ctx *c);
+void servers_detach(glint_ctx *c);
 
 inline ExactCtx make_exact(glint_ctx *c) {
     ExactCtx e;

@@ -353,299 +353,3 @@ extern "C" glint_status glint_active_search_noalloc(glint_ctx *c, const uint32_t
     return GLINT_OK;
 }
 
-/* ---- contact-trace queries over the flushed store -------------------------
- * Breadth-first expansion for a batch of queries at once.  Per query slot: a
- * visited bitmap over objects and two object lists (this hop's frontier and
- * the next).  One launch per hop covers every (query, frontier object,
- * block) triple: the object's sid in the block gives its CTF (or the
- * oversize buffer), first/count its keys, and each key is decoded as the
- * reference's CTF::parse_key does (tracing/step_merge.cpp:335-345). */
-namespace glint {
-
-constexpr uint32_t kQuerySlots = 64;
-constexpr uint32_t kMaxHops = 8;
-
-struct HopArgs {
-    const StoreBlockDev *blocks;
-    uint32_t nblocks;
-    uint32_t N;
-    uint64_t words;                      /* bitmap words per slot */
-    uint32_t *visited;
-    uint32_t *lists;                     /* [slot][2][N] */
-    uint32_t cur;                        /* which list is the frontier */
-    const unsigned long long *prefix;    /* [Q + 1] frontier sizes, prefix sums */
-    const uint32_t *qparam;              /* [Q][4] t_start, t_end, window */
-    uint32_t *counts;                    /* [Q] next-list sizes */
-    uint32_t Q;
-    unsigned long long *scanned;
-};
-
-__device__ inline void visit(const HopArgs &a, uint32_t q, uint32_t target) {
-    if (target >= a.N) return;
-    uint32_t *vis = a.visited + (size_t)q * a.words;
-    const uint32_t bit = 1u << (target & 31);
-    const uint32_t old = atomicOr(&vis[target >> 5], bit);
-    if (old & bit) return;
-    const uint32_t idx = atomicAdd(&a.counts[q], 1u);
-    if (idx < a.N) a.lists[((size_t)q * 2 + (a.cur ^ 1)) * a.N + idx] = target;
-}
-
-__global__ void __launch_bounds__(256) k_q_hop(HopArgs a) {
-    const unsigned long long total = a.prefix[a.Q] * a.nblocks;
-    unsigned long long scanned = 0;
-    for (unsigned long long it = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; it < total;
-         it += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned long long f = it / a.nblocks;
-        const uint32_t b = (uint32_t)(it - f * a.nblocks);
-        uint32_t lo = 0, hi = a.Q; /* the query: prefix[q] <= f < prefix[q + 1] */
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) / 2;
-            if (a.prefix[mid] <= f) lo = mid;
-            else hi = mid;
-        }
-        const uint32_t q = lo;
-        const uint32_t obj = a.lists[((size_t)q * 2 + a.cur) * a.N + (f - a.prefix[q])];
-        const StoreBlockDev blk = a.blocks[b];
-        const uint32_t sid = blk.sids[obj];
-        if (sid == 0) continue;
-        const uint32_t n = blk.count[obj], first = blk.first[obj];
-        const uint32_t t0 = a.qparam[4 * q], t1 = a.qparam[4 * q + 1], window = a.qparam[4 * q + 2];
-        scanned += n;
-        if (sid == 1) {
-            for (uint32_t j = 0; j < n; ++j) {
-                const ulonglong2 k = blk.okeys[first + j];
-                const uint32_t end = (uint32_t)k.x + blk.end_time_min, duration = (uint32_t)(k.x >> 32);
-                const uint32_t start = end - duration;
-                if (window && !(start < t1 && t0 < end)) continue;
-                visit(a, q, (uint32_t)k.y & ((1u << 26) - 1));
-            }
-            continue;
-        }
-        const uint32_t c = sid - 2;
-        if (c >= blk.C) continue;
-        const glint_ctf_meta m = blk.ctfs[c];
-        const uint32_t kb = m.key_bit / 8;
-        const uint8_t *base = blk.keys + blk.byte_index[c] + (unsigned long long)(first - blk.key_index[c]) * kb;
-        for (uint32_t j = 0; j < n; ++j) {
-            const uint8_t *p = base + (size_t)j * kb;
-            unsigned __int128 v = 0;
-            for (uint32_t t = 0; t < kb; ++t) v |= (unsigned __int128)p[t] << (8 * t);
-            v >>= m.mbr_bit;
-            const uint32_t end = (uint32_t)(v & ((1ull << m.end_bit) - 1)) + blk.end_time_min;
-            v >>= m.end_bit;
-            const uint32_t duration = (uint32_t)(v & ((1ull << m.duration_bit) - 1));
-            v >>= m.duration_bit;
-            const uint32_t target = (uint32_t)(v & ((1ull << m.id_bit) - 1));
-            const uint32_t start = end - duration;
-            if (window && !(start < t1 && t0 < end)) continue;
-            visit(a, q, target);
-        }
-    }
-    for (int o = 16; o > 0; o >>= 1) scanned += __shfl_down_sync(0xffffffffu, scanned, o);
-    if ((threadIdx.x & 31) == 0 && scanned) atomicAdd(a.scanned, scanned);
-}
-
-/* the seeds of every query: visited and listed as the first frontier */
-__global__ void k_q_seed(const uint32_t *__restrict__ seeds, const unsigned long long *__restrict__ sprefix, uint32_t Q,
-                         HopArgs a) {
-    const unsigned long long total = sprefix[Q];
-    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < total;
-         i += (unsigned long long)gridDim.x * blockDim.x) {
-        uint32_t lo = 0, hi = Q;
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) / 2;
-            if (sprefix[mid] <= i) lo = mid;
-            else hi = mid;
-        }
-        const uint32_t p = seeds[i];
-        if (p >= a.N) continue;
-        uint32_t *vis = a.visited + (size_t)lo * a.words;
-        const uint32_t bit = 1u << (p & 31);
-        if (atomicOr(&vis[p >> 5], bit) & bit) continue;
-        const uint32_t idx = atomicAdd(&a.counts[lo], 1u);
-        a.lists[((size_t)lo * 2 + a.cur) * a.N + idx] = p;
-    }
-}
-
-void query_pool_free(glint_ctx *c) {
-    QueryPool &p = c->qpool;
-    void *ps[] = {p.visited, p.lists, p.counts, p.seeds, p.prefix, p.qparam, p.blocks};
-    for (void *x : ps)
-        if (x) cudaFree(x);
-    p = QueryPool();
-}
-
-static cudaError_t query_pool_ensure(glint_ctx *c, uint32_t slots, uint64_t nseeds, uint32_t nblocks) {
-    QueryPool &p = c->qpool;
-    const uint64_t words = ((uint64_t)c->N + 31) / 32;
-    cudaError_t e = cudaSuccess;
-    if (p.slots < slots) {
-        void *ps[] = {p.visited, p.lists, p.counts, p.prefix, p.qparam};
-        for (void *x : ps)
-            if (x) cudaFree(x);
-        p.visited = p.lists = p.counts = p.qparam = nullptr;
-        p.prefix = nullptr;
-        p.slots = 0;
-        if ((e = cudaMalloc((void **)&p.visited, sizeof(uint32_t) * words * slots)) != cudaSuccess) return e;
-        if ((e = cudaMalloc((void **)&p.lists, sizeof(uint32_t) * 2 * (size_t)c->N * slots)) != cudaSuccess) return e;
-        if ((e = cudaMalloc((void **)&p.counts, sizeof(uint32_t) * slots)) != cudaSuccess) return e;
-        if ((e = cudaMalloc((void **)&p.prefix, sizeof(unsigned long long) * (2 * (slots + 1) + 1))) != cudaSuccess)
-            return e;
-        if ((e = cudaMalloc((void **)&p.qparam, sizeof(uint32_t) * 4 * slots)) != cudaSuccess) return e;
-        p.slots = slots;
-    }
-    if (p.seeds_cap < nseeds) {
-        if (p.seeds) cudaFree(p.seeds);
-        p.seeds = nullptr;
-        p.seeds_cap = 0;
-        if ((e = cudaMalloc((void **)&p.seeds, sizeof(uint32_t) * (nseeds ? nseeds : 1))) != cudaSuccess) return e;
-        p.seeds_cap = nseeds;
-    }
-    if (p.blocks_cap < nblocks) {
-        if (p.blocks) cudaFree(p.blocks);
-        p.blocks = nullptr;
-        p.blocks_cap = 0;
-        if ((e = cudaMalloc((void **)&p.blocks, sizeof(StoreBlockDev) * (nblocks ? nblocks : 1))) != cudaSuccess)
-            return e;
-        p.blocks_cap = nblocks;
-    }
-    return e;
-}
-
-/* one batch of at most kQuerySlots queries */
-static glint_status query_chunk(glint_ctx *c, const glint_query *qs, uint32_t Q, glint_query_result *rs) {
-    cudaStream_t s = c->stream;
-    const uint32_t nb = (uint32_t)c->ctbs.size();
-    uint64_t nseeds = 0;
-    uint32_t max_hops = 0;
-    for (uint32_t q = 0; q < Q; ++q) {
-        nseeds += qs[q].n_seeds;
-        max_hops = std::max(max_hops, std::min(qs[q].hops, kMaxHops));
-    }
-    cudaError_t e = query_pool_ensure(c, Q, nseeds, nb);
-    if (e != cudaSuccess) {
-        c->last_error = std::string("query scratch: ") + cudaGetErrorString(e);
-        return e == cudaErrorMemoryAllocation ? GLINT_ERR_OUT_OF_MEMORY : GLINT_ERR_CUDA;
-    }
-    QueryPool &p = c->qpool;
-    std::vector<StoreBlockDev> bd(nb);
-    for (uint32_t i = 0; i < nb; ++i) {
-        const StoreBlock &b = c->ctbs[i];
-        bd[i] = StoreBlockDev{b.keys, b.ctfs, b.key_index, b.byte_index, b.sids, b.first, b.count, b.okeys,
-                              b.end_time_min, c->cfg.CTF_count};
-    }
-    std::vector<uint32_t> seeds(nseeds ? nseeds : 1), qparam(4 * Q);
-    std::vector<unsigned long long> sprefix(Q + 1), prefix(Q + 1);
-    uint64_t at = 0;
-    for (uint32_t q = 0; q < Q; ++q) {
-        sprefix[q] = at;
-        if (qs[q].n_seeds) std::memcpy(seeds.data() + at, qs[q].seeds, sizeof(uint32_t) * qs[q].n_seeds);
-        at += qs[q].n_seeds;
-        qparam[4 * q] = qs[q].t_start;
-        qparam[4 * q + 1] = qs[q].t_end;
-        qparam[4 * q + 2] = (qs[q].t_start == 0 && qs[q].t_end == 0) ? 0u : 1u;
-        rs[q].n = 0;
-        rs[q].keys_scanned = 0;
-        for (uint32_t h = 0; h < kMaxHops; ++h) rs[q].hop_end[h] = 0;
-    }
-    sprefix[Q] = at;
-    const uint64_t words = ((uint64_t)c->N + 31) / 32;
-    unsigned long long *d_sprefix = p.prefix + (Q + 1);
-    unsigned long long *d_scanned = p.prefix + 2 * (Q + 1);
-    cudaMemsetAsync(d_scanned, 0, sizeof(unsigned long long), s);
-    cudaMemsetAsync(p.visited, 0, sizeof(uint32_t) * words * Q, s);
-    cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * Q, s);
-    if (nb) cudaMemcpyAsync(p.blocks, bd.data(), sizeof(StoreBlockDev) * nb, cudaMemcpyHostToDevice, s);
-    if (nseeds) cudaMemcpyAsync(p.seeds, seeds.data(), sizeof(uint32_t) * nseeds, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(d_sprefix, sprefix.data(), sizeof(unsigned long long) * (Q + 1), cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(p.qparam, qparam.data(), sizeof(uint32_t) * 4 * Q, cudaMemcpyHostToDevice, s);
-    HopArgs a;
-    a.blocks = p.blocks;
-    a.nblocks = nb;
-    a.N = c->N;
-    a.words = words;
-    a.visited = p.visited;
-    a.lists = p.lists;
-    a.cur = 0;
-    a.prefix = p.prefix;
-    a.qparam = p.qparam;
-    a.counts = p.counts;
-    a.Q = Q;
-    a.scanned = d_scanned;
-    if (nseeds) k_q_seed<<<grid_for(nseeds, 256), 256, 0, s>>>(p.seeds, d_sprefix, Q, a);
-    std::vector<uint32_t> cnt(Q);
-    cudaMemcpyAsync(cnt.data(), p.counts, sizeof(uint32_t) * Q, cudaMemcpyDeviceToHost, s);
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) {
-        c->last_error = std::string("query seeds: ") + cudaGetErrorString(e);
-        return GLINT_ERR_CUDA;
-    }
-    std::vector<uint32_t> buf;
-    for (uint32_t h = 0; h < max_hops; ++h) {
-        /* frontier sizes; finished queries expand nothing */
-        unsigned long long acc = 0;
-        for (uint32_t q = 0; q < Q; ++q) {
-            prefix[q] = acc;
-            acc += (h < qs[q].hops) ? cnt[q] : 0u;
-        }
-        prefix[Q] = acc;
-        cudaMemcpyAsync(p.prefix, prefix.data(), sizeof(unsigned long long) * (Q + 1), cudaMemcpyHostToDevice, s);
-        cudaMemsetAsync(p.counts, 0, sizeof(uint32_t) * Q, s);
-        a.cur = h & 1;
-        if (acc && nb) k_q_hop<<<grid_for(acc * nb, 256, 152u * 16u), 256, 0, s>>>(a);
-        cudaMemcpyAsync(cnt.data(), p.counts, sizeof(uint32_t) * Q, cudaMemcpyDeviceToHost, s);
-        if ((e = cudaStreamSynchronize(s)) != cudaSuccess) break;
-        for (uint32_t q = 0; q < Q; ++q) {
-            if (h >= qs[q].hops) {
-                cnt[q] = 0;
-                continue;
-            }
-            const uint32_t k = std::min(cnt[q], c->N);
-            glint_query_result &r = rs[q];
-            if (k) {
-                buf.resize(k);
-                e = cudaMemcpy(buf.data(), p.lists + ((size_t)q * 2 + (a.cur ^ 1)) * c->N, sizeof(uint32_t) * k,
-                               cudaMemcpyDeviceToHost);
-                if (e != cudaSuccess) break;
-                std::sort(buf.begin(), buf.end());
-                for (uint32_t i = 0; i < k; ++i)
-                    if (r.ids && r.n + i < r.cap) r.ids[r.n + i] = buf[i];
-            }
-            r.n += k;
-            r.hop_end[h] = r.n;
-        }
-        if (e != cudaSuccess) break;
-    }
-    unsigned long long scanned = 0;
-    if (e == cudaSuccess) e = cudaMemcpy(&scanned, d_scanned, sizeof(scanned), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) {
-        c->last_error = std::string("query: ") + cudaGetErrorString(e);
-        return GLINT_ERR_CUDA;
-    }
-    for (uint32_t q = 0; q < Q; ++q) {
-        rs[q].keys_scanned = q == 0 ? scanned : 0; /* per batch, reported on its first query */
-        for (uint32_t h = std::min(qs[q].hops, kMaxHops); h < kMaxHops; ++h) rs[q].hop_end[h] = rs[q].n;
-    }
-    return GLINT_OK;
-}
-
-} // namespace glint
-
-extern "C" glint_status glint_query_batch(glint_ctx *c, const glint_query *qs, uint32_t nq, glint_query_result *rs) {
-    if (!c || (nq && (!qs || !rs))) return GLINT_ERR_INVALID_ARGUMENT;
-    for (uint32_t q = 0; q < nq; ++q)
-        if ((qs[q].n_seeds && !qs[q].seeds) || qs[q].hops == 0 || qs[q].hops > kMaxHops)
-            return GLINT_ERR_INVALID_ARGUMENT;
-    cudaSetDevice(c->device);
-    cudaError_t e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess) {
-        c->last_error = std::string("query: ") + cudaGetErrorString(e);
-        return GLINT_ERR_CUDA;
-    }
-    for (uint32_t b = 0; b < nq; b += kQuerySlots) {
-        const glint_status st = query_chunk(c, qs + b, std::min(kQuerySlots, nq - b), rs + b);
-        if (st != GLINT_OK) return st;
-    }
-    return GLINT_OK;
-}
-
-extern "C" uint32_t glint_store_blocks(const glint_ctx *c) { return c ? (uint32_t)c->ctbs.size() : 0u; }

@@ -290,6 +290,27 @@ typedef struct glint_query_result {
 
 glint_status glint_query_batch(glint_ctx *ctx, const glint_query *queries, uint32_t num_queries,
                                glint_query_result *results);
+
+/* Serving form: continuous batching of contact-trace queries.  A server owns
+ * query slots (a visited bitmap and two frontier lists each); the number of
+ * slots is min(max_slots, what half of the free device memory holds).  Each
+ * glint_server_step admits queued queries into free slots, advances every
+ * active query by one hop in one launch, and retires the finished ones, so a
+ * query that arrives while others are in flight joins at the next step.  A
+ * query's result does not depend on what else is in flight.  The server
+ * reads the context's kept store blocks; one host thread drives it, between
+ * steps of the context. */
+typedef struct glint_server glint_server;
+glint_status glint_server_create(glint_ctx *ctx, uint32_t max_slots, glint_server **out);
+glint_status glint_server_destroy(glint_server *srv);
+uint32_t glint_server_slots(const glint_server *srv);
+/* queue a query (its seeds are copied); *ticket identifies it */
+glint_status glint_server_submit(glint_server *srv, const glint_query *query, uint64_t *ticket);
+/* one admission + hop + retirement round; optional counts after it */
+glint_status glint_server_step(glint_server *srv, uint32_t *active, uint32_t *queued);
+/* *done = 1 when the query has finished; its result is then written into r
+ * (ids up to r->cap) and the ticket is released */
+glint_status glint_server_poll(glint_server *srv, uint64_t ticket, glint_query_result *r, int *done);
 /* number of flushed blocks currently kept for queries */
 uint32_t glint_store_blocks(const glint_ctx *ctx);
 

@@ -18,6 +18,7 @@ def build_store(name, steps, flush_at, keep=16):
                       reach_distance=cfgd["reach_distance"], min_meet_time=cfgd["min_meet_time"],
                       schema_update_delay=cfgd["schema_update_delay"], kv_capacity=1 << 22, store_keep=keep)
     g = DeviceBench(c, box, pts[0])
+    g.map_box = np.asarray(box, np.float64)
     windows = []   # meetings of each flushed window
     cur = []
     for t in range(steps):
@@ -30,7 +31,13 @@ def build_store(name, steps, flush_at, keep=16):
     return g, cfgd["num_objects"], windows
 
 
-def edges_of(meetings):
+def edges_of(meetings, box=None):
+    if box is not None:
+        # only meetings whose f32 box lies inside the map become keys
+        # (box_contain, cuda/geometry.cu:53-58, 667-670)
+        b = meetings["mbr"].astype(np.float64)
+        inside = (b[:, 0] >= box[0]) & (b[:, 2] <= box[2]) & (b[:, 1] >= box[1]) & (b[:, 3] <= box[3])
+        meetings = meetings[inside]
     e = np.zeros(2 * len(meetings), EDGE_DTYPE)
     e["pid"][0::2], e["target"][0::2] = meetings["pid1"], meetings["pid2"]
     e["pid"][1::2], e["target"][1::2] = meetings["pid2"], meetings["pid1"]
@@ -51,7 +58,7 @@ def check(g, n, edges, queries):
 def test_query_matches_oracle_bfs():
     g, n, windows = build_store("dense_20k", 50, (20, 35, 49))
     assert g.store_blocks() == 3
-    edges = edges_of(np.concatenate(windows))
+    edges = edges_of(np.concatenate(windows), g.map_box)
     rng = np.random.default_rng(3)
     queries = []
     for k, hops, win in [(1, 3, (0, 0)), (10, 2, (0, 0)), (100, 1, (0, 0)), (1000, 3, (0, 0)), (50, 3, (10, 30)),
@@ -69,7 +76,54 @@ def test_query_matches_oracle_bfs():
 def test_query_kept_blocks_only():
     g, n, windows = build_store("dense_20k", 40, (12, 25, 39), keep=2)
     assert g.store_blocks() == 2
-    edges = edges_of(np.concatenate(windows[1:]))
+    edges = edges_of(np.concatenate(windows[1:]), g.map_box)
     rng = np.random.default_rng(4)
     check(g, n, edges, [(rng.choice(n, 300, replace=False).astype(np.uint32), 3, 0, 0)])
+    g.close()
+
+
+def test_serving_mix_equals_alone():
+    """Continuous batching: queries admitted while others are in flight, with
+    fewer slots than queries, give exactly their results alone (and the
+    oracle's)."""
+    from glint_pipeline_gb300 import Server
+    g, n, windows = build_store("dense_20k", 50, (20, 35, 49))
+    edges = edges_of(np.concatenate(windows), g.map_box)
+    rng = np.random.default_rng(9)
+    queries = []
+    for i in range(30):
+        k = int(np.exp(rng.uniform(0, np.log(1000))))
+        hops = int(rng.integers(1, 4))
+        if i % 3 == 0:
+            win = (0, 0)
+        else:
+            t0 = int(rng.integers(0, 45))
+            win = (t0, t0 + int(rng.integers(2, 30)))
+        queries.append((rng.choice(n, k, replace=False).astype(np.uint32), hops, win[0], win[1]))
+    alone = [g.query([q])[0][0] for q in queries]
+    srv = Server(g, max_slots=7)
+    assert srv.slots == 7
+    tickets = {}
+    pending = list(range(len(queries)))
+    results = {}
+    step = 0
+    while pending or len(results) < len(queries):
+        for _ in range(int(rng.integers(0, 5))):   # arrivals between steps
+            if pending:
+                i = pending.pop(0)
+                tickets[srv.submit(*queries[i])] = i
+        active, queued = srv.step()
+        for t, i in list(tickets.items()):
+            r = srv.poll(t)
+            if r is not None:
+                results[i] = r[0]
+                del tickets[t]
+        step += 1
+        assert step < 10_000
+    for i, (seeds, hops, t0, t1) in enumerate(queries):
+        want = query_bfs(edges, n, seeds, hops, t0, t1)
+        for h in range(hops):
+            np.testing.assert_array_equal(results[i][h], alone[i][h], err_msg=f"query {i} hop {h + 1} (mix vs alone)")
+            np.testing.assert_array_equal(results[i][h], want[h], err_msg=f"query {i} hop {h + 1} (vs oracle)")
+    srv.close()
     g.close()
