@@ -1,12 +1,16 @@
 """Benchmark: object-timesteps/s of the contact-tracing step at 10M objects.
 
-Workload (BASELINE configs[1]): the seeded Manhattan-grid generator, 10M
+Workload: the seeded Manhattan-grid generator (40x40 km, 8 hotspots), 10M
 objects, FP64 lon/lat, reach 2 m, minimum meeting 5 steps, QuadTree leaf
 capacity 50 (the reference default), a meeting table of 2^30 buckets.  One
-step = partition -> filter -> refine -> table insert -> identify -> schema
-update for one 1-second timestep of all objects.  Both forms produce
-bit-identical meetings; "plain" runs the reference's FP64 test on every
-candidate pair, "tuned" screens pairs in FP32 with a guard band first.
+step = partition -> filter -> refine -> table insert -> identify (+ keys) ->
+schema update for one 1-second timestep of all objects, plus the flush into
+the key-value store whenever more than kv_restriction keys are pending (as
+the reference's loop does).  Both forms produce bit-identical meetings;
+"plain" runs the reference's FP64 test on every candidate pair, "tuned"
+screens pairs in FP32 with a guard band first.  After the steps, the serving
+form answers a Poisson stream of contact-trace queries against the flushed
+store (p50/p99 latency, queries/s).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                     [--objects N] [--mode both|plain|tuned]
@@ -52,8 +56,12 @@ def parse():
     p.add_argument("--e2e-steps", type=int, default=8)
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
-    p.add_argument("--cpu-sample-objects", type=int, default=1_000_000)
+    p.add_argument("--cpu-sample-objects", type=int, default=500_000)
     p.add_argument("--cpu-sample-steps", type=int, default=3)
+    p.add_argument("--cpu-threads", type=int, default=0, help="0: all host cores")
+    p.add_argument("--serve-seconds", type=float, default=6.0)
+    p.add_argument("--serve-rate", type=float, default=200.0)
+    p.add_argument("--no-serve", action="store_true")
     return p.parse_args()
 
 
@@ -159,29 +167,30 @@ def cudart():
 
 
 def stage_bytes(stage, N, st, K):
-    """Algorithmic bytes of one launch of a stage's main kernel."""
+    """Algorithmic bytes of one step of a stage: per-unit figures x units."""
     if stage == "refine":
-        # member tiles x, y, L, id (28 B/object); per cross check the querier's
-        # x, y, L and the check (32 B); per contact one table record read
-        # (32 B), its box written back (16 B) and its stamp (1 B); per new pair
-        # a 16 B new-list entry
-        return 28 * N + 32 * st["cross_checks"] + 49 * st["contacts"] + 16 * st["new_keys"]
+        # member tile (X, Y, cx, f32 x/y, id: 32 B/object); per cross check the
+        # check and the querier's record (48 B); per contact the table record
+        # read (32 B), its box written (16 B) and its stamp (1 B); per new pair
+        # a 16-B new-list entry
+        return 32 * N + 48 * st["cross_checks"] + 49 * st["contacts"] + 16 * st["new_keys"]
     if stage == "identify":
-        # two stamp passes (2 B/bucket), per expiring entry its 16 B head read
-        # and 8 B write, per reported meeting the record (32 B) and log entry (32 B)
-        return 2 * st["buckets"] + 24 * st["expired"] + 64 * st["meetings"]
+        # stamps (2 B/bucket over two passes); per expiring entry its record
+        # read and reset (48 B); per new entry its finalisation (80 B); per
+        # reported meeting the record, log entry and two keys with boxes (128 B)
+        return 2 * st["buckets"] + 48 * st["expired"] + 80 * st["new_keys"] + 128 * st["meetings"]
     if stage == "filter":
-        # per object its leaf/last_valid/count (12 B); per border object its
-        # point and L (24 B); per check 8 B by querier + 8 B by target
-        return 12 * N + 24 * st["border_objects"] + 16 * st["cross_checks"]
+        # per object its leaf words and counts (24 B); per border object its
+        # coordinates and scale (36 B); per check 24 B over the two lists
+        return 24 * N + 36 * st["border_objects"] + 24 * st["cross_checks"]
     if stage == "insert":
-        # per new pair: list entry (16 B), record head CAS (32 B), stamp, then
-        # the finalize pass (16 B list + 32 B record + 32 B of points)
-        return 129 * st["new_keys"]
+        # per new pair: list entry (16 B), record compare-and-swap read and
+        # write (64 B), stamp (1 B)
+        return 81 * st["new_keys"]
     if stage == "partition":
-        # points (16 B) + leaf/last_valid/leaf node/L writes (20 B) + scatter (8 B)
-        # + gather (16+8+4 B in, 28 B out)
-        return 100 * N
+        # point and order reads, three leaf words, scatter, segment sort, and
+        # the gather of six per-object arrays
+        return 124 * N
     return 0
 
 
@@ -192,13 +201,14 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
     lib = _abi.lib()
     K, W = args.steps, max(args.warmup, 3)
     cfg = gp.Configuration(num_objects=N, num_meeting_buckets=args.buckets, device=local, timing=True,
-                           precision_mode=1 if mode == "tuned" else 0)
+                           precision_mode=1 if mode == "tuned" else 0, auto_flush=True)
     bench = gp.DeviceBench(cfg, box, first)
     for t in range(W):
         bench.step_device(dbuf.value + t * step_bytes, t)
         bench.sync()
     barrier(pg)
     stage_ms = np.zeros(8)
+    flush_ms, flushes = 0.0, 0
     acc = {"candidates": 0, "contacts": 0, "new_keys": 0, "meetings": 0, "cross_checks": 0, "border_objects": 0,
            "taken": 0, "active": 0, "band_pairs": 0, "rechecks": 0, "ambiguous": 0}
     launches = 0
@@ -209,7 +219,9 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
             bench.step_device(dbuf.value + t * step_bytes, t)
             st = bench.sync()
             stage_ms += np.array(st.ms)
-            dev_ms += st.ms[7]
+            dev_ms += st.ms[7] + st.flush_ms
+            flush_ms += st.flush_ms
+            flushes += int(st.flushed)
             launches += st.launches
             acc["candidates"] += st.candidates
             acc["contacts"] += st.contacts
@@ -230,13 +242,17 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
     per["checks"] = last.checks
     per["leaves"] = last.leaves
     per["error_flags"] = last.error_flags
+    stage = {k: v / K for k, v in zip(STAGES, stage_ms)}
+    stage["flush"] = flush_ms / K
+    stage["total"] = stage["total"] + stage["flush"]
+    per["flushes"] = flushes
     out = {"value": N * K * world / dev_s, "ms_per_step": 1000.0 * dev_s / K,
-           "stage_ms": {k: v / K for k, v in zip(STAGES, stage_ms)}, "per_step": per,
+           "stage_ms": stage, "per_step": per,
            "clocks": clk.summary(), "gpu_launches": launches}
 
     if args.no_e2e:
         out["e2e"] = None
-        bench.close()
+        out["_bench"] = bench
         return out
     # e2e: continue the trajectory with host-resident points
     ke = max(1, min(args.e2e_steps, K))
@@ -271,7 +287,7 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
                   "d2h_bytes_per_step": int(d2h / ke), "steps": ke}
     del host, arr
     rt.cudaFreeHost(hbuf)
-    bench.close()
+    out["_bench"] = bench
     return out
 
 
@@ -289,53 +305,124 @@ def roofline(form, N):
             "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "of fallback"}
 
 
-def cpu_baseline(args):
-    """The CPU oracle (C restatement of the reference's stages) on a bounded sample."""
+def cpu_baseline(args, steps=None, warm=1):
+    """The reference's CPU stages (the oracle's C restatement, -O2) on the
+    host cores: one independent instance per thread, each on its own sample
+    of the same generator; value = all threads' object-timesteps / wall time.
+    ctypes releases the GIL around every step, so the threads run in
+    parallel."""
+    import threading
     from glint_pipeline_gb300.tracegen import SEED_SCALE, TraceGenerator
     from oracle.bindings import Oracle, make_config
-    n, k = args.cpu_sample_objects, args.cpu_sample_steps
-    g = TraceGenerator(SEED_SCALE, n)
-    box, pts = g.box(), g.steps(k + 1)
-    o = Oracle(make_config(n, num_meeting_buckets=1 << 24), box, pts[0])
-    o.step(pts[0], 0)
+    n = args.cpu_sample_objects
+    k = steps if steps is not None else args.cpu_sample_steps
+    threads = args.cpu_threads or os.cpu_count() or 1
+    inst = []
+    for i in range(threads):
+        g = TraceGenerator(SEED_SCALE + 0x100 * i, n)
+        box, pts = g.box(), g.steps(warm + k)
+        o = Oracle(make_config(n, num_meeting_buckets=1 << 23), box, pts[0])
+        for t in range(warm):
+            o.step(pts[t], t)
+        inst.append((o, pts))
+    barrier = threading.Barrier(threads + 1)
+
+    def run(o, pts):
+        barrier.wait()
+        for t in range(warm, warm + k):
+            o.step(pts[t], t)
+
+    ths = [threading.Thread(target=run, args=x) for x in inst]
+    for th in ths:
+        th.start()
+    barrier.wait()
     t0 = time.perf_counter()
-    for t in range(1, k + 1):
-        o.step(pts[t], t)
+    for th in ths:
+        th.join()
     dt = time.perf_counter() - t0
-    o.close()
-    return {"value": n * k / dt, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"{n} objects of the same generator (seed, box, hotspots), {k} timed steps after one; "
-                      f"single-threaded C restatement of the reference's CPU stages (-O2)"}
+    for o, _ in inst:
+        o.close()
+    return {"value": threads * n * k / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{threads} threads x {n} objects of the same generator (one seed per thread), {k} timed "
+                      f"steps after {warm}; the reference's CPU stages as the single-threaded C restatement, one "
+                      f"instance per thread", "ms_per_step": 1000.0 * dt / k}
 
 
 def run_reference_arm(args, rank, world, pg):
     if rank != 0:
         return
-    from glint_pipeline_gb300.tracegen import SEED_SCALE, TraceGenerator
-    from oracle.bindings import Oracle, make_config
-    n = args.cpu_sample_objects
-    g = TraceGenerator(SEED_SCALE, n)
-    steps = max(1, min(args.steps, 5))
-    warm = max(1, min(args.warmup, 3))
-    box, pts = g.box(), g.steps(warm + steps)
-    o = Oracle(make_config(n, num_meeting_buckets=1 << 24), box, pts[0])
-    for t in range(warm):
-        o.step(pts[t], t)
-    t0 = time.perf_counter()
-    for t in range(warm, warm + steps):
-        o.step(pts[t], t)
-    dt = time.perf_counter() - t0
-    value = n * steps / dt
+    steps = max(1, min(args.steps, 3))
+    warm = max(1, min(args.warmup, 2))
+    cb = cpu_baseline(args, steps=steps, warm=warm)
+    value = cb["value"]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": steps, "warmup": warm, "ms_per_step": 1000 * dt / steps, "higher_is_better": True,
+            "steps": steps, "warmup": warm, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"Manhattan-grid generator (configs[1] generator), {n}-object sample, reach 2 m, "
-                                   f"min meeting 5, leaf capacity 50", "objects": n},
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                             "sample": f"{n} objects x {steps} steps; the reference's sources are not on this "
-                                       f"machine, so its CPU stages run as the single-threaded C restatement"},
+            "config": {"workload": f"Manhattan-grid generator, {cb['cores']} x {args.cpu_sample_objects}-object "
+                                   f"samples, reach 2 m, min meeting 5, leaf capacity 50",
+                       "objects": args.cpu_sample_objects},
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def serving(args, bench, N, t_hi):
+    """Poisson stream of contact-trace queries against the flushed store,
+    served with continuous batching; plus 2-hop queries from 1000 seeds
+    alone."""
+    import glint_pipeline_gb300 as gp
+    if bench.store_blocks() == 0:
+        return None
+    rng = np.random.default_rng(0x474C494E54000005)
+    srv = gp.Server(bench, max_slots=64)
+    n = max(1, int(args.serve_rate * args.serve_seconds))
+    arrive = np.cumsum(rng.exponential(1.0 / args.serve_rate, n))
+    qs = []
+    for _ in range(n):
+        k = int(np.exp(rng.uniform(0, np.log(1000))))
+        hops = int(rng.integers(1, 4))
+        length = float(np.exp(rng.uniform(np.log(10), np.log(1800))))
+        t0 = int(rng.integers(0, max(1, t_hi)))
+        qs.append((rng.choice(N, k, replace=False).astype(np.uint32), hops, t0, t0 + int(length)))
+    lat, inflight, i = [], {}, 0
+    reached = 0
+    t_start = time.perf_counter()
+    while len(lat) < n:
+        now = time.perf_counter() - t_start
+        while i < n and arrive[i] <= now:
+            inflight[srv.submit(*qs[i])] = arrive[i]
+            i += 1
+        if not inflight:
+            time.sleep(max(0.0, arrive[i] - now))
+            continue
+        srv.step()
+        done_t = time.perf_counter() - t_start
+        for tk in list(inflight):
+            r = srv.poll(tk, cap=1)
+            if r is not None:
+                lat.append(done_t - inflight.pop(tk))
+                reached += r[2]
+    wall = time.perf_counter() - t_start
+    lat = np.array(lat) * 1000.0
+    # 2-hop queries from 1000 seeds, one at a time
+    two = []
+    for _ in range(20):
+        seeds = rng.choice(N, 1000, replace=False).astype(np.uint32)
+        t0 = time.perf_counter()
+        tk = srv.submit(seeds, 2)
+        r = None
+        while r is None:
+            srv.step()
+            r = srv.poll(tk, cap=1)
+        two.append((time.perf_counter() - t0) * 1000.0)
+    srv.close()
+    two = np.array(two)
+    return {"queries": n, "rate_req_s": args.serve_rate, "qps": n / wall, "p50_ms": float(np.percentile(lat, 50)),
+            "p99_ms": float(np.percentile(lat, 99)), "slots": srv.slots, "store_blocks": bench.store_blocks(),
+            "mean_reached": reached / n,
+            "mix": "seeds 1-1000 log-uniform, 1-3 hops, window 10-1800 s log-uniform",
+            "two_hop_1k_seeds": {"p50_ms": float(np.percentile(two, 50)), "p99_ms": float(np.percentile(two, 99)),
+                                 "queries": len(two)}}
 
 
 def main():
@@ -369,8 +456,13 @@ def main():
 
     modes = ["tuned", "plain"] if args.mode == "both" else [args.mode]
     forms = {}
+    serve = None
     for m in modes:
         forms[m] = run_form(args, m, N, local, pg, world, box, first, pb, ob, dbuf, step_bytes, rt)
+        b = forms[m].pop("_bench")
+        if m == modes[0] and not args.no_serve:
+            serve = serving(args, b, N, total)
+        b.close()
     rt.cudaFree(dbuf)
     head = forms[modes[0]]
     cpu = cpu_baseline(args) if (rank == 0 and world == 1 and not args.no_cpu) else None
@@ -378,12 +470,13 @@ def main():
         line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
                 "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64", "data": "synthetic",
-                "config": {"workload": f"Manhattan-grid generator (configs[1]): {N} objects, FP64 lon/lat, reach 2 m, "
-                                       f"min meeting 5, leaf capacity 50, {args.buckets} buckets; headline form "
-                                       f"'{modes[0]}'", "objects": N, "buckets": args.buckets, "form": modes[0],
+                "config": {"workload": f"Manhattan-grid generator (40x40 km, 8 hotspots): {N} objects, FP64 "
+                                       f"lon/lat, reach 2 m, min meeting 5, leaf capacity 50, {args.buckets} "
+                                       f"buckets, flush past 2^26 keys; headline form '{modes[0]}'",
+                           "objects": N, "buckets": args.buckets, "form": modes[0],
                            "l2": "inputs larger than L2 (160 MB of points per step, 34 GB table)"},
                 "roofline": roofline(head, N), "clocks": head["clocks"], "e2e": head["e2e"], "cpu_baseline": cpu,
-                "gpu_launches": head["gpu_launches"],
+                "gpu_launches": head["gpu_launches"], "serving": serve,
                 "forms": {m: {k: v for k, v in f.items()} for m, f in forms.items()}}
         print(json.dumps(line), flush=True)
 

@@ -62,7 +62,7 @@ class Configuration:
     split_num: int = 10
     store_keep: int = 16                # flushed blocks kept on the device for queries
     kv_restriction: int = 0             # 0 -> G_bytes * 2^25 keys (config.h:80)
-    kv_capacity: int = 0                # 0 -> kv_restriction + 1000000 (config.h:81)
+    kv_capacity: int = 0                # 0 -> kv_restriction + max(1e6, 4 N)
 
     def to_c(self) -> GlintConfig:
         c = GlintConfig()

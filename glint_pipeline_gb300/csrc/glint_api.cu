@@ -333,7 +333,10 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     c->y_buffer = cfg.y_buffer != 0 ? cfg.y_buffer : cfg.reach_distance * c->dpm_lat;
     /* key-value store sizes (util/config.h:77-85) and the first window */
     c->kv_restriction = cfg.kv_restriction ? cfg.kv_restriction : (uint64_t)cfg.G_bytes * 33554432ull;
-    c->kv_cap = cfg.kv_capacity ? cfg.kv_capacity : c->kv_restriction + 1000000;
+    /* the reference adds 1e6 keys of headroom (util/config.h:81), which one
+     * step of 10M objects (~13M keys) overruns: allow 4 keys per object */
+    c->kv_cap = cfg.kv_capacity ? cfg.kv_capacity
+                                : c->kv_restriction + std::max<uint64_t>(1000000, 4ull * cfg.num_objects);
     c->end_time_min = cfg.start_time + cfg.min_meet_time; /* tracing/process.cpp:404 */
     /* decisions within 2^-38 relative of the threshold are re-taken exactly */
     c->band = cfg.reach_distance * std::ldexp(1.0, -38);

@@ -93,7 +93,8 @@ typedef struct glint_config {
     uint32_t store_keep;           /* flushed blocks (CTBs) kept on the device for glint_query_batch;
                                       0 -> none; the oldest is dropped first */
     uint64_t kv_restriction;       /* 0 -> G_bytes*2^25 keys (util/config.h:80) */
-    uint64_t kv_capacity;          /* key buffer; 0 -> kv_restriction + 1000000 (util/config.h:81) */
+    uint64_t kv_capacity;          /* key buffer; 0 -> kv_restriction + max(1000000, 4*num_objects)
+                                      (util/config.h:81 adds 1000000) */
 } glint_config;
 
 typedef struct glint_box {
