@@ -29,9 +29,12 @@ constexpr uint64_t kKeyMask = (1ULL << 62) - 1;
 
 enum : uint8_t { kInvalid = 0, kBranch = 1, kLeaf = 2 }; /* index/QTree.h:43-47 */
 
-/* stamp byte per table slot: 0 empty, 1/2 committed entry touched at an even/odd
- * step, 3 entry inserted during the current step */
-enum : uint8_t { kStampEmpty = 0, kStampNew = 3 };
+/* stamp byte per table slot: 0 empty, 1 committed entry, 3 entry inserted
+ * during the current step (4: reported this step, identify only).  Which step
+ * last touched a committed entry is its tag, 1 or 2 by step parity, in the
+ * high half of the record's w1 (the low half holds the start time), so a
+ * touch writes only the record it has just read. */
+enum : uint8_t { kStampEmpty = 0, kStampOld = 1, kStampNew = 3 };
 __host__ __device__ inline uint8_t stamp_of(uint64_t step_index) { return (uint8_t)(1 + (step_index & 1)); }
 
 /* ---- exact comparisons without the FP64 pipe --------------------------------
@@ -91,7 +94,7 @@ static_assert(sizeof(DNode) == 64, "DNode must be 64 bytes");
  * instead of the Cantor key, which is equivalent and needs no inverse.
  * w0: (a << 32) | b (committed), kNewFlag | (a << 32) | b (inserted this
  *     step) or kEmptyW0
- * w1: start time (committed) or insertion priority (new)
+ * w1: (touch tag << 32) | start time (committed) or insertion priority (new)
  * mbr: order-preserving encodings of the f32 box (low x, low y, high x, high y) */
 struct __align__(32) TRec {
     unsigned long long w0;
@@ -101,6 +104,10 @@ struct __align__(32) TRec {
 static_assert(sizeof(TRec) == 32, "TRec must be 32 bytes");
 constexpr unsigned long long kEmptyW0 = ~0ull;
 constexpr unsigned long long kPairMask = ~kNewFlag;
+
+/* the touch tag of a committed record */
+__device__ inline uint32_t rec_tag(const TRec &r) { return (uint32_t)(r.w1 >> 32); }
+__device__ inline void rec_set_tag(TRec &r, uint32_t tag) { reinterpret_cast<uint32_t *>(&r.w1)[1] = tag; }
 
 __host__ __device__ inline unsigned long long pair_word(uint32_t a, uint32_t b) {
     return ((unsigned long long)a << 32) | b;
@@ -353,16 +360,15 @@ __device__ inline Screen make_screen(float cx, const Frame &f) {
  * 1.5*2^23 + v exactly, so one subtraction recovers v */
 __device__ inline float small_to_f(int v) { return __fsub_rn(__int_as_float(0x4B400000 + v), 12582912.0f); }
 
-/* correctly rounded FP32 value of d */
+/* correctly rounded FP32 value of d for |d| < 2^44; NaN beyond (2^13
+ * map widths apart), which sends the test to the exact path */
 __device__ inline float fx_to_f(long long d) {
-    const long long s = 1ll << 22, w = 1ll << 44;
-    if (d > -s && d < s) return small_to_f((int)d);
-    if (d > -w && d < w) {
-        /* d = hi 2^22 + lo with lo in [0, 2^22): one rounding in the fma */
-        const int hi = (int)(d >> 22), lo = (int)(d & 0x3FFFFF);
-        return __fmaf_rn(small_to_f(hi), 4194304.0f, small_to_f(lo));
-    }
-    return __ll2float_rn(d);
+    /* d = hi 2^22 + lo with lo in [0, 2^22): one rounding in the fma; for
+     * |d| < 2^22, hi is 0 or -1 and the fma is exact */
+    const long long w = 1ll << 44;
+    const int hi = (int)(d >> 22), lo = (int)(d & 0x3FFFFF);
+    const float f = __fmaf_rn(small_to_f(hi), 4194304.0f, small_to_f(lo));
+    return (d > -w && d < w) ? f : __int_as_float(0x7fc00000);
 }
 
 /* 1 within reach, 0 beyond, -1 inside the guard band (or a NaN scale);

@@ -10,82 +10,78 @@
  *
  * Device form: a stamp byte per bucket says empty / touched at this step /
  * touched at the previous step, so the scan reads one byte per bucket and the
- * 32-byte record only of entries that expire.  Pass 1 (16 buckets per thread)
- * removes expired entries that are too short, marks the ones to report and
- * counts them per 8192-bucket tile; an exclusive scan gives every tile its
- * offset; pass 2 visits only tiles with reports and writes them in bucket
- * order into the device meeting log, then removes those entries.
+ * 32-byte record only of entries that change.  Pass 1 (32 consecutive buckets
+ * per warp and round) finalises entries inserted this step, removes expired
+ * entries that are too short, marks the ones to report and counts them per
+ * 8192-bucket tile; an exclusive scan gives every tile its offset; pass 2
+ * visits only tiles with reports and writes them in bucket order into the
+ * device meeting log, then removes those entries.
  */
 #include "glint_internal.cuh"
 
 namespace glint {
 
-constexpr int kIdThreads = 512;
-constexpr int kIdItems = 16;
-constexpr uint32_t kIdTile = kIdThreads * kIdItems;
+constexpr int kIdThreads = 256;
+constexpr uint32_t kIdWarpSpan = 1024;                      /* buckets per warp, 32 rounds of 32 */
+constexpr uint32_t kIdTile = (kIdThreads / 32) * kIdWarpSpan; /* 8192 buckets per block */
 constexpr uint8_t kStampEmit = 4;
 
+/* Pass 1.  Warp w of a block walks buckets tile + w*1024 + round*32 + lane,
+ * so each round reads 32 consecutive stamps and, where needed, 32
+ * consecutive records: the records of one round share DRAM lines. */
 __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict__ stamp, TRec *__restrict__ tab,
                                                              uint64_t B, uint8_t st_now, uint32_t cur_time,
                                                              uint32_t min_plus1, uint32_t *__restrict__ tile_cnt,
                                                              const float2 *__restrict__ fpos, uint32_t N,
                                                              DevCounters *cnt) {
     __shared__ uint32_t red[3][kIdThreads / 32];
-    const uint64_t base = (uint64_t)blockIdx.x * kIdTile + (uint64_t)threadIdx.x * kIdItems;
-    uint32_t emit = 0, taken = 0, active = 0;
-    if (base < B) {
-        uint4 s4 = *reinterpret_cast<const uint4 *>(stamp + base); /* B is padded to a multiple of 16 */
-        uint32_t w[4] = {s4.x, s4.y, s4.z, s4.w};
-        bool changed = false;
-#pragma unroll
-        for (int k = 0; k < kIdItems; ++k) {
-            const uint32_t sh = 8 * (k & 3);
-            const uint8_t sv = (uint8_t)(w[k >> 2] >> sh);
-            if (sv == kStampEmpty || base + k >= B) continue;
-            ++taken;
-            if (sv == st_now) {
-                ++active;
-                continue;
-            }
-            TRec &r = tab[base + k];
-            if (sv == kStampNew) {
-                /* a pair inserted this step: start = now and the f32 box of
-                 * its two points (geometry.cu:481-489) */
-                ++active;
-                const unsigned long long pw = r.w0 & kPairMask;
-                const uint32_t pa = pair_a(pw), pb = pair_b(pw);
-                TRec nr;
-                nr.w0 = pw;
-                nr.w1 = cur_time;
-                if (pa < N && pb < N) {
-                    const float2 A = fpos[pa], Bp = fpos[pb];
-                    const float ax = A.x, ay = A.y, bx = Bp.x, by = Bp.y;
-                    nr.mbr[0] = min(fenc(ax), fenc(bx));
-                    nr.mbr[1] = min(fenc(ay), fenc(by));
-                    nr.mbr[2] = max(fenc(ax), fenc(bx));
-                    nr.mbr[3] = max(fenc(ay), fenc(by));
-                } else {
-                    atomicOr(&cnt->error_flags, GLINT_EF_DUPLICATE_NEW);
-                    nr.mbr[0] = nr.mbr[1] = nr.mbr[2] = nr.mbr[3] = 0;
-                }
-                r = nr;
-                w[k >> 2] = (w[k >> 2] & ~(0xffu << sh)) | ((uint32_t)st_now << sh);
-                changed = true;
-                continue;
-            }
-            const uint32_t start = (uint32_t)r.w1;
-            if (cur_time - start >= min_plus1) {
-                ++emit;
-                w[k >> 2] = (w[k >> 2] & ~(0xffu << sh)) | ((uint32_t)kStampEmit << sh);
-            } else {
-                *reinterpret_cast<ulonglong2 *>(&r) = make_ulonglong2(kEmptyW0, 0ull);
-                w[k >> 2] &= ~(0xffu << sh);
-            }
-            changed = true;
-        }
-        if (changed) *reinterpret_cast<uint4 *>(stamp + base) = make_uint4(w[0], w[1], w[2], w[3]);
-    }
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint64_t wbase = (uint64_t)blockIdx.x * kIdTile + (uint64_t)wid * kIdWarpSpan;
+    uint32_t emit = 0, taken = 0, active = 0;
+    for (uint32_t round = 0; round < kIdWarpSpan / 32; ++round) {
+        const uint64_t b = wbase + round * 32 + lane;
+        if (b >= B) break;
+        const uint8_t sv = stamp[b];
+        if (sv == kStampEmpty) continue;
+        ++taken;
+        TRec &r = tab[b];
+        if (sv == kStampNew) {
+            /* a pair inserted this step: start = now and the f32 box of its
+             * two points (geometry.cu:481-489) */
+            ++active;
+            const unsigned long long pw = r.w0 & kPairMask;
+            const uint32_t pa = pair_a(pw), pb = pair_b(pw);
+            TRec nr;
+            nr.w0 = pw;
+            nr.w1 = ((unsigned long long)st_now << 32) | cur_time;
+            if (pa < N && pb < N) {
+                const float2 A = fpos[pa], Bp = fpos[pb];
+                nr.mbr[0] = min(fenc(A.x), fenc(Bp.x));
+                nr.mbr[1] = min(fenc(A.y), fenc(Bp.y));
+                nr.mbr[2] = max(fenc(A.x), fenc(Bp.x));
+                nr.mbr[3] = max(fenc(A.y), fenc(Bp.y));
+            } else {
+                atomicOr(&cnt->error_flags, GLINT_EF_DUPLICATE_NEW);
+                nr.mbr[0] = nr.mbr[1] = nr.mbr[2] = nr.mbr[3] = 0;
+            }
+            r = nr;
+            stamp[b] = kStampOld;
+            continue;
+        }
+        const unsigned long long w1 = r.w1;
+        if ((uint32_t)(w1 >> 32) == st_now) {
+            ++active;
+            continue;
+        }
+        const uint32_t start = (uint32_t)w1;
+        if (cur_time - start >= min_plus1) {
+            ++emit;
+            stamp[b] = kStampEmit;
+        } else {
+            *reinterpret_cast<ulonglong2 *>(&r) = make_ulonglong2(kEmptyW0, 0ull);
+            stamp[b] = kStampEmpty;
+        }
+    }
     for (int o = 16; o > 0; o >>= 1) {
         emit += __shfl_down_sync(0xffffffffu, emit, o);
         taken += __shfl_down_sync(0xffffffffu, taken, o);
@@ -110,6 +106,8 @@ __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict
     }
 }
 
+/* Pass 2: the reports of tiles that have any, in bucket order (warps in
+ * order, rounds in order, lanes in order), into the meeting log */
 __global__ void __launch_bounds__(kIdThreads) k_expire_emit(uint8_t *__restrict__ stamp, TRec *__restrict__ tab,
                                                             uint64_t B, uint32_t cur_time,
                                                             const uint32_t *__restrict__ tile_cnt,
@@ -118,58 +116,43 @@ __global__ void __launch_bounds__(kIdThreads) k_expire_emit(uint8_t *__restrict_
                                                             const DevCounters *cnt) {
     if (tile_cnt[blockIdx.x] == 0) return; /* uniform per block */
     __shared__ uint32_t ws[kIdThreads / 32];
-    const uint64_t base = (uint64_t)blockIdx.x * kIdTile + (uint64_t)threadIdx.x * kIdItems;
-    uint32_t w[4] = {0, 0, 0, 0};
-    uint32_t mine = 0;
-    if (base < B) {
-        uint4 s4 = *reinterpret_cast<const uint4 *>(stamp + base);
-        w[0] = s4.x; w[1] = s4.y; w[2] = s4.z; w[3] = s4.w;
-#pragma unroll
-        for (int k = 0; k < kIdItems; ++k)
-            if ((uint8_t)(w[k >> 2] >> (8 * (k & 3))) == kStampEmit) mine |= 1u << k;
-    }
-    /* block exclusive scan of the per-thread report counts */
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const uint32_t v = (uint32_t)__popc(mine);
-    uint32_t x = v;
-    for (int o = 1; o < 32; o <<= 1) {
-        uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
-        if (lane >= o) x += y;
+    const uint64_t wbase = (uint64_t)blockIdx.x * kIdTile + (uint64_t)wid * kIdWarpSpan;
+    uint32_t mine = 0;
+    for (uint32_t round = 0; round < kIdWarpSpan / 32; ++round) {
+        const uint64_t b = wbase + round * 32 + lane;
+        if (b < B && stamp[b] == kStampEmit) ++mine;
     }
-    if (lane == 31) ws[wid] = x;
+    for (int o = 16; o > 0; o >>= 1) mine += __shfl_xor_sync(0xffffffffu, mine, o);
+    if (lane == 0) ws[wid] = mine;
     __syncthreads();
-    if (wid == 0) {
-        uint32_t s = lane < kIdThreads / 32 ? ws[lane] : 0u;
-        for (int o = 1; o < 32; o <<= 1) {
-            uint32_t y = __shfl_up_sync(0xffffffffu, s, o);
-            if (lane >= o) s += y;
-        }
-        if (lane < kIdThreads / 32) ws[lane] = s;
-    }
-    __syncthreads();
-    if (!mine) return;
-    uint32_t pos = tile_off[blockIdx.x] + (wid ? ws[wid - 1] : 0u) + x - v;
+    uint32_t pos = tile_off[blockIdx.x];
+    for (int w = 0; w < wid; ++w) pos += ws[w];
+    if (mine == 0) return;
     const unsigned long long head = cnt->log_head;
-    for (int k = 0; k < kIdItems; ++k) {
-        if (!(mine & (1u << k))) continue;
-        TRec &r = tab[base + k];
-        const unsigned long long w0 = r.w0;
-        const uint4 m = *reinterpret_cast<const uint4 *>(r.mbr);
-        glint_meeting out;
-        out.pid1 = pair_a(w0);
-        out.pid2 = pair_b(w0);
-        out.start = (uint32_t)r.w1;
-        out.end = cur_time - 1;
-        out.mbr[0] = fdec(m.x);
-        out.mbr[1] = fdec(m.y);
-        out.mbr[2] = fdec(m.z);
-        out.mbr[3] = fdec(m.w);
-        log[(head + pos) % log_cap] = out;
-        ++pos;
-        *reinterpret_cast<ulonglong2 *>(&r) = make_ulonglong2(kEmptyW0, 0ull);
-        w[k >> 2] &= ~(0xffu << (8 * (k & 3)));
+    for (uint32_t round = 0; round < kIdWarpSpan / 32; ++round) {
+        const uint64_t b = wbase + round * 32 + lane;
+        const bool e = b < B && stamp[b] == kStampEmit;
+        const unsigned m = __ballot_sync(0xffffffffu, e);
+        if (e) {
+            TRec &r = tab[b];
+            const unsigned long long w0 = r.w0;
+            const uint4 mb = *reinterpret_cast<const uint4 *>(r.mbr);
+            glint_meeting out;
+            out.pid1 = pair_a(w0);
+            out.pid2 = pair_b(w0);
+            out.start = (uint32_t)r.w1;
+            out.end = cur_time - 1;
+            out.mbr[0] = fdec(mb.x);
+            out.mbr[1] = fdec(mb.y);
+            out.mbr[2] = fdec(mb.z);
+            out.mbr[3] = fdec(mb.w);
+            log[(head + pos + __popc(m & ((1u << lane) - 1u))) % log_cap] = out;
+            *reinterpret_cast<ulonglong2 *>(&r) = make_ulonglong2(kEmptyW0, 0ull);
+            stamp[b] = kStampEmpty;
+        }
+        pos += __popc(m);
     }
-    *reinterpret_cast<uint4 *>(stamp + base) = make_uint4(w[0], w[1], w[2], w[3]);
 }
 
 __global__ void k_identify_advance(const uint32_t *__restrict__ tile_off, uint64_t tiles, uint64_t log_cap,

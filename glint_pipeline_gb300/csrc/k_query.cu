@@ -10,7 +10,8 @@
  *
  * Device form, run after a step against the table it left: the listed ids
  * become a bitmap of N bits; pass 1 reads the stamp byte of every bucket and
- * the record only of buckets touched at the last step, and counts matching
+ * the record of occupied buckets (its tag says whether the last step touched
+ * it), and counts matching
  * sides per 8192-bucket tile; an exclusive scan gives each tile its offset;
  * pass 2 writes the records in bucket order.  The output order is therefore
  * deterministic.
@@ -33,7 +34,7 @@ struct SearchArgs {
     const TRec *tab;
     const uint8_t *stamp;
     uint64_t B;
-    uint8_t st;              /* stamp of entries touched at the last step */
+    uint8_t st;              /* tag of entries touched at the last step */
     uint32_t cur_time;
     uint32_t min_plus1;
     const uint32_t *bits;
@@ -56,7 +57,7 @@ __device__ inline bool listed(const SearchArgs &a, uint32_t p) {
  * id, bit 1 the higher id */
 __device__ inline uint32_t search_sides(const SearchArgs &a, uint64_t slot, TRec &r) {
     r = a.tab[slot];
-    if (r.w0 == kEmptyW0 || (r.w0 & kNewFlag)) return 0;
+    if (r.w0 == kEmptyW0 || (r.w0 & kNewFlag) || rec_tag(r) != a.st) return 0;
     if (a.cur_time - (uint32_t)r.w1 < a.min_plus1) return 0;
     return (listed(a, pair_a(r.w0)) ? 1u : 0u) | (listed(a, pair_b(r.w0)) ? 2u : 0u);
 }
@@ -69,7 +70,7 @@ __device__ inline uint32_t search_thread_masks(const SearchArgs &a, uint64_t bas
     const uint32_t w[4] = {s4.x, s4.y, s4.z, s4.w};
 #pragma unroll
     for (int k = 0; k < kSearchItems; ++k) {
-        if ((uint8_t)(w[k >> 2] >> (8 * (k & 3))) != a.st || base + k >= a.B) continue;
+        if ((uint8_t)(w[k >> 2] >> (8 * (k & 3))) != kStampOld || base + k >= a.B) continue;
         TRec r;
         masks |= search_sides(a, base + k, r) << (2 * k);
     }

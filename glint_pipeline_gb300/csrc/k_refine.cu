@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ lis
                     /* the carried pair's own committed entry */
                     const uint32_t pa = pair_a(plain), pb = pair_b(plain);
                     if (pa < N && pb < N) touch_box(tab[slot], fpos[pa], fpos[pb]);
-                    stamp[slot] = st;
+                    rec_set_tag(tab[slot], st);
                     done = true;
                     break;
                 }

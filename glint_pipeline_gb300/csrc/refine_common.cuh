@@ -47,7 +47,7 @@ struct RefineArgs {
 };
 
 /* The table as it stood at the start of the step: keys do not change while
- * the refine kernels run.  Found -> touch the entry (stamp, f32 box; each pair
+ * the refine kernels run.  Found -> touch the entry (tag, f32 box; each pair
  * has at most one event per step, so the box needs no atomics).  Not found
  * before an empty slot -> the pair is new this step. */
 __device__ inline bool table_touch(const RefineArgs &a, const QEntry &q) {
@@ -65,7 +65,7 @@ __device__ inline bool table_touch(const RefineArgs &a, const QEntry &q) {
                 m.w = max(m.w, hy);
                 *reinterpret_cast<uint4 *>(a.tab[slot].mbr) = m;
             }
-            a.stamp[slot] = a.st;
+            rec_set_tag(a.tab[slot], a.st);
             return false;
         }
         if (w0 == kEmptyW0) return true;
