@@ -210,7 +210,7 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
     stage_ms = np.zeros(8)
     flush_ms, flushes = 0.0, 0
     acc = {"candidates": 0, "contacts": 0, "new_keys": 0, "meetings": 0, "cross_checks": 0, "border_objects": 0,
-           "taken": 0, "active": 0, "band_pairs": 0, "rechecks": 0, "ambiguous": 0}
+           "taken": 0, "active": 0, "band_pairs": 0, "box_band": 0, "rechecks": 0, "ambiguous": 0}
     launches = 0
     dev_ms = 0.0
     last = None
@@ -232,6 +232,7 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
             acc["taken"] += st.num_taken_buckets
             acc["active"] += st.num_active_meetings
             acc["band_pairs"] += st.band_pairs
+            acc["box_band"] += st.box_band
             acc["rechecks"] += st.rechecks
             acc["ambiguous"] += st.ambiguous
             last = st

@@ -99,6 +99,8 @@ class GlintStepStats(ctypes.Structure):
         ("kv_count", ctypes.c_uint64),
         ("flushed", ctypes.c_uint32),
         ("flush_ms", ctypes.c_float),
+        ("box_band", ctypes.c_uint32),
+        ("reserved1", ctypes.c_uint32),
     ]
 
     def as_dict(self):

@@ -28,6 +28,8 @@ void schema_set_attributes();
 size_t refine_smem_bytes(uint32_t cap);
 uint64_t identify_tiles(uint64_t B);
 cudaError_t noalloc_setup(int device);
+/* stamps cover a whole number of identify tiles (the padding stays empty) */
+inline uint64_t stamp_bytes(uint64_t B) { return identify_tiles(B) * 8192 + 64; }
 } // namespace glint
 
 using namespace glint;
@@ -401,7 +403,7 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     ALLOC(c->d_tcursor, G);
     ALLOC(c->d_tlist, c->check_cap);
     ALLOC(c->d_tab, c->B);
-    ALLOC(c->d_stamp, (c->B + 16));
+    ALLOC(c->d_stamp, stamp_bytes(c->B));
     ALLOC(c->d_new, c->new_cap);
     ALLOC(c->d_tile_cnt, c->n_tiles + 1);
     ALLOC(c->d_tile_off, c->n_tiles + 1);
@@ -496,7 +498,7 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     init_sin_coef(&coef);
     cudaMemcpy(c->d_coef, &coef, sizeof(coef), cudaMemcpyHostToDevice);
     k_fill_empty<<<grid_for(c->B, 256, 152u * 16u), 256, 0, c->stream>>>(c->d_tab, c->B);
-    cudaMemsetAsync(c->d_stamp, 0, c->B + 16, c->stream);
+    cudaMemsetAsync(c->d_stamp, 0, stamp_bytes(c->B), c->stream);
     cudaMemsetAsync(c->d_grid_count, 0, sizeof(uint32_t) * ((size_t)G + 1), c->stream);
     k_iota<<<grid_for(N, 256, 152u * 8u), 256, 0, c->stream>>>(c->d_order, N);
     /* scratch address of glint_active_search_noalloc, once per device, with
@@ -599,6 +601,7 @@ static void fill_stats(glint_ctx *c, glint_step_stats *st) {
     st->rechecks = h.rechecks;
     st->ambiguous = h.ambiguous;
     st->band_pairs = h.band_pairs;
+    st->box_band = h.box_band;
     st->error_flags = h.error_flags;
     /* kernels per step: partition 9, filter 9, refine 1, insert 1,
      * identify 6 + keys 1, schema update 11, tail 1 (scans count three each) */

@@ -392,13 +392,17 @@ __host__ __device__ inline IBox fx_box(double lx, double ly, double hx, double h
 
 /* box distance screening: the gap from the point to the box along each axis */
 __device__ inline int fx_box_screen(const IBox &b, long long px, long long py, const Screen &s, float cy) {
-    long long dx = b.x - px;
-    if (px - b.z > dx) dx = px - b.z;
-    if (dx < 0) dx = 0;
-    long long dy = b.y - py;
-    if (py - b.w > dy) dy = py - b.w;
-    if (dy < 0) dy = 0;
-    return fx_screen(dx, dy, s, cy);
+    /* the gaps are taken after the conversion: rounding is monotonic, so the
+     * FP32 maximum is the rounded integer maximum (and needs no 64-bit max) */
+    const float x1 = fx_to_f(b.x - px), x2 = fx_to_f(px - b.z);
+    const float y1 = fx_to_f(b.y - py), y2 = fx_to_f(py - b.w);
+    if (!(x1 == x1 && x2 == x2 && y1 == y1 && y2 == y2)) return -1; /* beyond fx_to_f's range */
+    const float gx = fmaxf(fmaxf(x1, x2), 0.0f), gy = fmaxf(fmaxf(y1, y2), 0.0f);
+    const float mx = gx * s.cx, my = gy * cy;
+    const float q = mx * mx + my * my;
+    if (q < s.lo) return 1;
+    if (q > s.hi) return 0;
+    return -1;
 }
 
 /* box::width(true) > two_r (geometry/geometry.h:166-172), exact */

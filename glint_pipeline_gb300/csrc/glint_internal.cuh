@@ -46,6 +46,7 @@ struct DevCounters {
     unsigned int rechecks;
     unsigned int ambiguous;
     unsigned int band_pairs;
+    unsigned int box_band;
     unsigned int error_flags;
     unsigned int n_leaf_work;              /* leaves with at least one object */
     unsigned int work_next;                /* dynamic scheduling cursor */
@@ -53,7 +54,7 @@ struct DevCounters {
     unsigned int n_cand;                   /* merge candidates this step */
     unsigned int total_checks;
     unsigned int n_big;                    /* leaf segments sorted by a whole block */
-    unsigned int pad[3];
+    unsigned int pad[2];
     /* persistent (not cleared per step) */
     unsigned int ssi;                      /* schema_stack_index */
     unsigned int gsi;                      /* grids_stack_index */

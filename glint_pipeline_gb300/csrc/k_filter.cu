@@ -75,6 +75,7 @@ __device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const do
         double2 lo;
         bool have_lo = false;
         if (in < 0) {
+            atomicAdd(&cnt->box_band, 1u);
             lo = low[ch];
             have_lo = true;
             if (Lp == 0.0) Lp = dpm_lon_fast(w.py);

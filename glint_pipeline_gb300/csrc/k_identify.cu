@@ -28,58 +28,78 @@ constexpr uint8_t kStampEmit = 4;
 
 /* Pass 1.  Warp w of a block walks buckets tile + w*1024 + round*32 + lane,
  * so each round reads 32 consecutive stamps and, where needed, 32
- * consecutive records: the records of one round share DRAM lines. */
+ * consecutive records: the records of one round share DRAM lines.  The
+ * warp's 1024 stamps are staged in shared memory with one coalesced load, and
+ * the records of kIdIlp rounds are requested before any is used. */
+constexpr int kIdIlp = 4;
+
 __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict__ stamp, TRec *__restrict__ tab,
                                                              uint64_t B, uint8_t st_now, uint32_t cur_time,
                                                              uint32_t min_plus1, uint32_t *__restrict__ tile_cnt,
                                                              const float2 *__restrict__ fpos, uint32_t N,
                                                              DevCounters *cnt) {
     __shared__ uint32_t red[3][kIdThreads / 32];
+    __shared__ __align__(16) uint8_t sst[kIdThreads / 32][kIdWarpSpan];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint64_t wbase = (uint64_t)blockIdx.x * kIdTile + (uint64_t)wid * kIdWarpSpan;
+    /* stamps are allocated to a whole number of tiles */
+    const uint4 *src = reinterpret_cast<const uint4 *>(stamp + wbase);
+    uint4 *dst = reinterpret_cast<uint4 *>(sst[wid]);
+    dst[lane] = src[lane];
+    dst[lane + 32] = src[lane + 32];
+    __syncwarp();
     uint32_t emit = 0, taken = 0, active = 0;
-    for (uint32_t round = 0; round < kIdWarpSpan / 32; ++round) {
-        const uint64_t b = wbase + round * 32 + lane;
-        if (b >= B) break;
-        const uint8_t sv = stamp[b];
-        if (sv == kStampEmpty) continue;
-        ++taken;
-        TRec &r = tab[b];
-        if (sv == kStampNew) {
-            /* a pair inserted this step: start = now and the f32 box of its
-             * two points (geometry.cu:481-489) */
-            ++active;
-            const unsigned long long pw = r.w0 & kPairMask;
-            const uint32_t pa = pair_a(pw), pb = pair_b(pw);
-            TRec nr;
-            nr.w0 = pw;
-            nr.w1 = ((unsigned long long)st_now << 32) | cur_time;
-            if (pa < N && pb < N) {
-                const float2 A = fpos[pa], Bp = fpos[pb];
-                nr.mbr[0] = min(fenc(A.x), fenc(Bp.x));
-                nr.mbr[1] = min(fenc(A.y), fenc(Bp.y));
-                nr.mbr[2] = max(fenc(A.x), fenc(Bp.x));
-                nr.mbr[3] = max(fenc(A.y), fenc(Bp.y));
-            } else {
-                atomicOr(&cnt->error_flags, GLINT_EF_DUPLICATE_NEW);
-                nr.mbr[0] = nr.mbr[1] = nr.mbr[2] = nr.mbr[3] = 0;
+    for (uint32_t r0 = 0; r0 < kIdWarpSpan / 32; r0 += kIdIlp) {
+        uint8_t sv[kIdIlp];
+        ulonglong2 rec[kIdIlp];
+#pragma unroll
+        for (int u = 0; u < kIdIlp; ++u) {
+            const uint32_t off = (r0 + u) * 32 + lane;
+            sv[u] = wbase + off < B ? sst[wid][off] : kStampEmpty;
+            if (sv[u] != kStampEmpty) rec[u] = *reinterpret_cast<const ulonglong2 *>(&tab[wbase + off]);
+        }
+#pragma unroll
+        for (int u = 0; u < kIdIlp; ++u) {
+            if (sv[u] == kStampEmpty) continue;
+            const uint64_t b = wbase + (r0 + u) * 32 + lane;
+            ++taken;
+            TRec &r = tab[b];
+            if (sv[u] == kStampNew) {
+                /* a pair inserted this step: start = now and the f32 box of
+                 * its two points (geometry.cu:481-489) */
+                ++active;
+                const unsigned long long pw = rec[u].x & kPairMask;
+                const uint32_t pa = pair_a(pw), pb = pair_b(pw);
+                TRec nr;
+                nr.w0 = pw;
+                nr.w1 = ((unsigned long long)st_now << 32) | cur_time;
+                if (pa < N && pb < N) {
+                    const float2 A = fpos[pa], Bp = fpos[pb];
+                    nr.mbr[0] = min(fenc(A.x), fenc(Bp.x));
+                    nr.mbr[1] = min(fenc(A.y), fenc(Bp.y));
+                    nr.mbr[2] = max(fenc(A.x), fenc(Bp.x));
+                    nr.mbr[3] = max(fenc(A.y), fenc(Bp.y));
+                } else {
+                    atomicOr(&cnt->error_flags, GLINT_EF_DUPLICATE_NEW);
+                    nr.mbr[0] = nr.mbr[1] = nr.mbr[2] = nr.mbr[3] = 0;
+                }
+                r = nr;
+                stamp[b] = kStampOld;
+                continue;
             }
-            r = nr;
-            stamp[b] = kStampOld;
-            continue;
-        }
-        const unsigned long long w1 = r.w1;
-        if ((uint32_t)(w1 >> 32) == st_now) {
-            ++active;
-            continue;
-        }
-        const uint32_t start = (uint32_t)w1;
-        if (cur_time - start >= min_plus1) {
-            ++emit;
-            stamp[b] = kStampEmit;
-        } else {
-            *reinterpret_cast<ulonglong2 *>(&r) = make_ulonglong2(kEmptyW0, 0ull);
-            stamp[b] = kStampEmpty;
+            const unsigned long long w1 = rec[u].y;
+            if ((uint32_t)(w1 >> 32) == st_now) {
+                ++active;
+                continue;
+            }
+            const uint32_t start = (uint32_t)w1;
+            if (cur_time - start >= min_plus1) {
+                ++emit;
+                stamp[b] = kStampEmit;
+            } else {
+                *reinterpret_cast<ulonglong2 *>(&r) = make_ulonglong2(kEmptyW0, 0ull);
+                stamp[b] = kStampEmpty;
+            }
         }
     }
     for (int o = 16; o > 0; o >>= 1) {

@@ -164,6 +164,8 @@ typedef struct glint_step_stats {
     uint64_t kv_count;             /* keys pending for the next flush (workbench::kv_count) */
     uint32_t flushed;              /* 1: this step ended with an automatic flush */
     float flush_ms;                /* its device time (not included in ms[7]) */
+    uint32_t box_band;             /* filter box tests inside the FP32 guard band (re-taken in FP64) */
+    uint32_t reserved1;
 } glint_step_stats;
 
 typedef struct glint_ctx glint_ctx;
