@@ -48,6 +48,13 @@ __device__ inline WalkPoint walk_point(const double2 p, const longlong2 ip, floa
     return w;
 }
 
+/* the reference's FP64 box test for a box inside the guard band (rare); kept
+ * out of line so that none of its FP64 work is scheduled on the common path */
+__device__ __noinline__ bool box_exact(double lx, double ly, double hx, double hy, double px, double py,
+                                       const ExactCtx &ex) {
+    return box_le_exact(lx, ly, hx, hy, px, py, dpm_lon_fast(py), ex);
+}
+
 /* lookup_rec from node `start`; calls emit(gid, ordinal) in walk order;
  * returns the number of leaves kept.  The box test is screened on the
  * fixed-point boxes; only a box within the guard band of the reach takes the
@@ -63,7 +70,6 @@ __device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const do
     st_next[0] = 0;
     sp = 1;
     uint32_t kept = 0;
-    double Lp = 0.0; /* degree_per_meter_longitude(py), computed on first need */
     while (sp > 0) {
         const int top = sp - 1;
         const uint8_t i = st_next[top];
@@ -78,8 +84,7 @@ __device__ inline uint32_t lookup_walk(const DNode *__restrict__ nodes, const do
             atomicAdd(&cnt->box_band, 1u);
             lo = low[ch];
             have_lo = true;
-            if (Lp == 0.0) Lp = dpm_lon_fast(w.py);
-            in = box_le_exact(lo.x, lo.y, kdbl(n.khx), kdbl(n.khy), w.px, w.py, Lp, ex) ? 1 : 0;
+            in = box_exact(lo.x, lo.y, kdbl(n.khx), kdbl(n.khy), w.px, w.py, ex) ? 1 : 0;
         }
         if (in) {
             if (n.type == kLeaf) {

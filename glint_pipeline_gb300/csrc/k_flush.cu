@@ -84,14 +84,27 @@ __global__ void __launch_bounds__(256) k_keys_append(const glint_meeting *__rest
                                                      KeyArgs a, DevCounters *cnt) {
     const uint32_t total = cnt->meetings;
     const unsigned long long begin = cnt->log_step_begin;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
-        const glint_meeting m = log[(begin + i) % log_cap];
-        /* box_contain (cuda/geometry.cu:53-58, 667-670) */
-        if (!((double)m.mbr[0] >= a.map[0] && (double)m.mbr[2] <= a.map[2] && (double)m.mbr[1] >= a.map[1] &&
-              (double)m.mbr[3] <= a.map[3])) {
-            atomicAdd(&cnt->keys_outside, 1u);
-            continue;
+    const int lane = threadIdx.x & 31;
+    for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 - lane < total; i0 += gridDim.x * blockDim.x) {
+        const uint32_t i = i0;
+        glint_meeting m;
+        bool keep = false;
+        if (i < total) {
+            m = log[(begin + i) % log_cap];
+            /* box_contain (cuda/geometry.cu:53-58, 667-670) */
+            keep = (double)m.mbr[0] >= a.map[0] && (double)m.mbr[2] <= a.map[2] && (double)m.mbr[1] >= a.map[1] &&
+                   (double)m.mbr[3] <= a.map[3];
+            if (!keep) atomicAdd(&cnt->keys_outside, 1u);
         }
+        /* two keys per kept meeting, reserved once per warp */
+        const unsigned km = __ballot_sync(0xffffffffu, keep);
+        unsigned long long wbase = 0;
+        if (km) {
+            const int leader = __ffs(km) - 1;
+            if (lane == leader) wbase = atomicAdd(&cnt->kv_count, 2ull * __popc(km));
+            wbase = __shfl_sync(0xffffffffu, wbase, leader);
+        }
+        if (!keep) continue;
         const uint32_t duration = m.end - m.start;
         uint32_t pid = m.pid1, target = m.pid2;
         if (duration > a.max_meet) {
@@ -99,7 +112,7 @@ __global__ void __launch_bounds__(256) k_keys_append(const glint_meeting *__rest
             a.sids[pid] = 1;
             a.sids[target] = 1;
         }
-        const unsigned long long idx = atomicAdd(&cnt->kv_count, 2ull);
+        const unsigned long long idx = wbase + 2ull * __popc(km & ((1u << lane) - 1u));
         if (idx + 2 > a.cap) {
             atomicOr(&cnt->error_flags, GLINT_EF_KV_OVERFLOW);
             continue;
