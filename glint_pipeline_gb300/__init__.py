@@ -61,6 +61,7 @@ class Configuration:
     auto_flush: bool = False
     split_num: int = 10
     store_keep: int = 16                # flushed blocks kept on the device for queries
+    use_graph: bool = False             # capture the step as a CUDA graph
     kv_restriction: int = 0             # 0 -> G_bytes * 2^25 keys (config.h:80)
     kv_capacity: int = 0                # 0 -> kv_restriction + max(1e6, 4 N)
 

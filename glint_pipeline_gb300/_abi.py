@@ -53,6 +53,8 @@ class GlintConfig(ctypes.Structure):
         ("store_keep", ctypes.c_uint32),
         ("kv_restriction", ctypes.c_uint64),
         ("kv_capacity", ctypes.c_uint64),
+        ("use_graph", ctypes.c_uint32),
+        ("reserved2", ctypes.c_uint32),
     ]
 
 

@@ -185,6 +185,9 @@ void free_all(glint_ctx *c) {
     server_free_default(c);
     servers_detach(c);
     if (c->h_cnt) cudaFreeHost(c->h_cnt);
+    if (c->h_params) cudaFreeHost(c->h_params);
+    if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+    if (c->graph) cudaGraphDestroy(c->graph);
     if (c->timers.created) {
         for (auto &e : c->timers.ev) cudaEventDestroy(e);
         for (auto &e : c->flush_ev) cudaEventDestroy(e);
@@ -422,6 +425,13 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
         delete c;
         return st;
     }
+    if ((e = cudaMallocHost((void **)&c->h_params, sizeof(StepParams))) != cudaSuccess) {
+        glint_status st = cuda_fail(c, e, "cudaMallocHost");
+        free_all(c);
+        delete c;
+        return st;
+    }
+    std::memset(c->h_params, 0, sizeof(StepParams));
     if ((e = cudaMallocHost((void **)&c->h_cnt, sizeof(DevCounters))) != cudaSuccess) {
         glint_status st = cuda_fail(c, e, "cudaMallocHost");
         free_all(c);
@@ -545,13 +555,13 @@ glint_status glint_get_capacities(const glint_ctx *c, uint32_t *sc, uint32_t *gc
     return GLINT_OK;
 }
 
-static glint_status enqueue_step(glint_ctx *c, const double *points, bool host, uint32_t cur_time) {
+/* the launches of one step, from the counter reset to the copy of the
+ * counters to the host; no host synchronisation, so it can be captured */
+static void launch_step(glint_ctx *c, const double *points, bool host) {
     cudaStream_t s = c->stream;
-    const bool tm = c->cfg.timing != 0;
-    if (c->step_index > 0) std::swap(c->d_order, c->d_sorted);
-    c->step_index++;
-    c->last_time = cur_time;
+    const bool tm = c->cfg.timing != 0 && !c->cfg.use_graph;
     cudaMemsetAsync(c->d_cnt, 0, kStepCounterBytes, s);
+    cudaMemcpyAsync(&c->d_cnt->step_time, c->h_params, sizeof(StepParams), cudaMemcpyHostToDevice, s);
     if (tm) cudaEventRecord(c->timers.ev[0], s);
     if (host) {
         cudaMemcpyAsync(c->d_pts, points, sizeof(double2) * c->N, cudaMemcpyHostToDevice, s);
@@ -559,22 +569,55 @@ static glint_status enqueue_step(glint_ctx *c, const double *points, bool host, 
         cudaMemcpyAsync(c->d_pts, points, sizeof(double2) * c->N, cudaMemcpyDeviceToDevice, s);
     }
     if (tm) cudaEventRecord(c->timers.ev[1], s);
-    launch_partition(c, cur_time);
+    launch_partition(c, 0);
     if (tm) cudaEventRecord(c->timers.ev[2], s);
     launch_filter(c);
     if (tm) cudaEventRecord(c->timers.ev[3], s);
-    launch_refine(c, cur_time);
+    launch_refine(c, 0);
     if (tm) cudaEventRecord(c->timers.ev[4], s);
-    launch_insert(c, cur_time);
+    launch_insert(c, 0);
     if (tm) cudaEventRecord(c->timers.ev[5], s);
-    launch_identify(c, cur_time);
+    launch_identify(c, 0);
     launch_keys(c);
     if (tm) cudaEventRecord(c->timers.ev[6], s);
     if (c->cfg.dynamic_schema) launch_schema_update(c);
     k_step_tail<<<1, 1, 0, s>>>(c->d_qstart, c->N, c->d_cnt);
     if (tm) cudaEventRecord(c->timers.ev[7], s);
     cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, s);
+}
+
+static glint_status enqueue_step(glint_ctx *c, const double *points, bool host, uint32_t cur_time) {
+    cudaStream_t s = c->stream;
+    /* a captured step reads its parameters from host memory when it runs:
+     * the previous step must have finished before they are overwritten */
+    if (c->cfg.use_graph && c->step_index > 0) cudaStreamSynchronize(s);
+    c->step_index++;
+    c->last_time = cur_time;
+    c->h_params->step_time = cur_time;
+    c->h_params->step_tag = stamp_of(c->step_index);
+    c->h_params->end_time_min = c->end_time_min;
     c->stats_valid = false;
+    if (!c->cfg.use_graph || host) {
+        launch_step(c, points, host);
+    } else {
+        if (c->graph_exec && c->graph_src != (const void *)points) {
+            cudaGraphExecDestroy(c->graph_exec);
+            cudaGraphDestroy(c->graph);
+            c->graph_exec = nullptr;
+            c->graph = nullptr;
+        }
+        if (!c->graph_exec) {
+            cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+            if (e != cudaSuccess) return cuda_fail(c, e, "step capture");
+            launch_step(c, points, false);
+            e = cudaStreamEndCapture(s, &c->graph);
+            if (e == cudaSuccess) e = cudaGraphInstantiate(&c->graph_exec, c->graph, 0);
+            if (e != cudaSuccess) return cuda_fail(c, e, "step capture");
+            c->graph_src = points;
+        }
+        cudaError_t e = cudaGraphLaunch(c->graph_exec, s);
+        if (e != cudaSuccess) return cuda_fail(c, e, "step graph");
+    }
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(c, e, "step launch");
     return GLINT_OK;
@@ -610,7 +653,7 @@ static void fill_stats(glint_ctx *c, glint_step_stats *st) {
     st->kv_count = h.kv_count;
     st->flushed = c->last_flushed ? 1u : 0u;
     st->flush_ms = c->last_flush_ms;
-    if (c->cfg.timing) {
+    if (c->cfg.timing && !c->cfg.use_graph) {
         for (int k = 0; k < 7; ++k) cudaEventElapsedTime(&st->ms[k], c->timers.ev[k], c->timers.ev[k + 1]);
         cudaEventElapsedTime(&st->ms[7], c->timers.ev[0], c->timers.ev[7]);
     }

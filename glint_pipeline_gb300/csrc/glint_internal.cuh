@@ -65,6 +65,15 @@ struct DevCounters {
     unsigned int oversize_oid_count;
     unsigned int keys_outside;             /* meetings outside the map box (not keyed) */
     unsigned int pad2[3];
+    /* this step's parameters, copied in at the start of the step so that a
+     * captured step graph reads them from here */
+    unsigned int step_time;                /* cur_time */
+    unsigned int step_tag;                 /* touch tag of this step (1 or 2) */
+    unsigned int end_time_min;             /* base of key end offsets */
+    unsigned int pad3;
+};
+struct StepParams {
+    unsigned int step_time, step_tag, end_time_min, pad3;
 };
 /* bytes cleared at the start of every step */
 constexpr size_t kStepCounterBytes = offsetof(DevCounters, ssi);
@@ -223,6 +232,10 @@ struct glint_ctx {
     void *d_scan_tmp = nullptr;
     size_t scan_tmp_bytes = 0;
     double2 *h_stage = nullptr;            /* pinned staging for host points (optional) */
+    glint::StepParams *h_params = nullptr; /* pinned: the next step's parameters */
+    cudaGraph_t graph = nullptr;           /* the captured step (glint_config.use_graph) */
+    cudaGraphExec_t graph_exec = nullptr;
+    const void *graph_src = nullptr;       /* input buffer the graph copies from */
     glint::StepTimers timers;
     glint_step_stats last_stats;
     bool stats_valid = false;

@@ -76,7 +76,6 @@ struct KeyArgs {
     uint16_t *sids;
     double map[4];
     uint32_t max_meet;
-    uint32_t end_time_min;
 };
 
 /* the meetings this step wrote to the log become keys */
@@ -84,6 +83,7 @@ __global__ void __launch_bounds__(256) k_keys_append(const glint_meeting *__rest
                                                      KeyArgs a, DevCounters *cnt) {
     const uint32_t total = cnt->meetings;
     const unsigned long long begin = cnt->log_step_begin;
+    const uint32_t end_time_min = cnt->end_time_min;
     const int lane = threadIdx.x & 31;
     for (uint32_t i0 = blockIdx.x * blockDim.x + threadIdx.x; i0 - lane < total; i0 += gridDim.x * blockDim.x) {
         const uint32_t i = i0;
@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(256) k_keys_append(const glint_meeting *__rest
                 target = t;
             }
             a.keys[idx + k] = ((u128)pid << kPidShift) + ((u128)target << 64) + ((u128)duration << 32) +
-                              (u128)(uint32_t)(m.end - a.end_time_min);
+                              (u128)(uint32_t)(m.end - end_time_min);
             a.boxes[idx + k] = box;
             if (atomicAdd(&a.same[pid], 1u) == 0) atomicAdd(&cnt->sid_count, 1u);
             uint32_t *o = reinterpret_cast<uint32_t *>(&a.obox[pid]);
@@ -701,7 +701,6 @@ KeyArgs key_args(glint_ctx *c) {
     a.map[2] = c->mbr.high[0];
     a.map[3] = c->mbr.high[1];
     a.max_meet = c->cfg.max_meet_time;
-    a.end_time_min = c->end_time_min;
     return a;
 }
 

@@ -34,14 +34,15 @@ constexpr uint8_t kStampEmit = 4;
 constexpr int kIdIlp = 4;
 
 __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict__ stamp, TRec *__restrict__ tab,
-                                                             uint64_t B, uint8_t st_now, uint32_t cur_time,
-                                                             uint32_t min_plus1, uint32_t *__restrict__ tile_cnt,
+                                                             uint64_t B, uint32_t min_plus1,
+                                                             uint32_t *__restrict__ tile_cnt,
                                                              const float2 *__restrict__ fpos, uint32_t N,
                                                              DevCounters *cnt) {
     __shared__ uint32_t red[3][kIdThreads / 32];
     __shared__ __align__(16) uint8_t sst[kIdThreads / 32][kIdWarpSpan];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint64_t wbase = (uint64_t)blockIdx.x * kIdTile + (uint64_t)wid * kIdWarpSpan;
+    const uint32_t cur_time = cnt->step_time, st_now = cnt->step_tag;
     /* stamps are allocated to a whole number of tiles */
     const uint4 *src = reinterpret_cast<const uint4 *>(stamp + wbase);
     uint4 *dst = reinterpret_cast<uint4 *>(sst[wid]);
@@ -129,7 +130,7 @@ __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict
 /* Pass 2: the reports of tiles that have any, in bucket order (warps in
  * order, rounds in order, lanes in order), into the meeting log */
 __global__ void __launch_bounds__(kIdThreads) k_expire_emit(uint8_t *__restrict__ stamp, TRec *__restrict__ tab,
-                                                            uint64_t B, uint32_t cur_time,
+                                                            uint64_t B,
                                                             const uint32_t *__restrict__ tile_cnt,
                                                             const uint32_t *__restrict__ tile_off,
                                                             glint_meeting *__restrict__ log, uint64_t log_cap,
@@ -150,6 +151,7 @@ __global__ void __launch_bounds__(kIdThreads) k_expire_emit(uint8_t *__restrict_
     for (int w = 0; w < wid; ++w) pos += ws[w];
     if (mine == 0) return;
     const unsigned long long head = cnt->log_head;
+    const uint32_t cur_time = cnt->step_time;
     for (uint32_t round = 0; round < kIdWarpSpan / 32; ++round) {
         const uint64_t b = wbase + round * 32 + lane;
         const bool e = b < B && stamp[b] == kStampEmit;
@@ -187,15 +189,15 @@ __global__ void k_identify_advance(const uint32_t *__restrict__ tile_off, uint64
 uint64_t identify_tiles(uint64_t B) { return (B + kIdTile - 1) / kIdTile; }
 
 cudaError_t launch_identify(glint_ctx *c, uint32_t cur_time) {
+    (void)cur_time;
     cudaStream_t s = c->stream;
     const uint64_t tiles = identify_tiles(c->B);
-    const uint8_t st_now = stamp_of(c->step_index);
     const uint32_t min_plus1 = c->cfg.min_meet_time + 1;
-    k_expire_count<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, st_now, cur_time, min_plus1,
-                                                          c->d_tile_cnt, c->d_fpos, c->N, c->d_cnt);
+    k_expire_count<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, min_plus1, c->d_tile_cnt,
+                                                          c->d_fpos, c->N, c->d_cnt);
     scan_u32(c->d_tile_cnt, c->d_tile_off, tiles, c->d_scan_tmp, s);
-    k_expire_emit<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, cur_time, c->d_tile_cnt,
-                                                         c->d_tile_off, c->d_log, c->log_cap, c->d_cnt);
+    k_expire_emit<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, c->d_tile_cnt, c->d_tile_off,
+                                                         c->d_log, c->log_cap, c->d_cnt);
     k_identify_advance<<<1, 1, 0, s>>>(c->d_tile_off, tiles, c->log_cap, c->d_cnt);
     return cudaGetLastError();
 }

@@ -259,6 +259,8 @@ cudaError_t launch_partition(glint_ctx *c, uint32_t /*cur_time*/) {
     o.fpos = c->d_fpos;
     o.rank_of = c->d_rank_of;
     k_gather<<<grid_for(N, 256, 152u * 8u), 256, 0, s>>>(c->d_sorted, N, c->d_pts, o, c->frame);
+    /* this step's leaf-major order is the next descent's processing order */
+    cudaMemcpyAsync(c->d_order, c->d_sorted, sizeof(uint32_t) * N, cudaMemcpyDeviceToDevice, s);
     return cudaGetLastError();
 }
 

@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(32 * kPrecWarps) k_refine_fp32(RefineArgs a) {
     uint32_t band = 0;
     uint32_t qn = 0;
     const uint32_t nwork = a.cnt->n_leaf_work;
+    const uint32_t tag = a.cnt->step_tag;
     for (;;) {
         uint32_t li = 0;
         if (lane == 0) li = atomicAdd(&a.cnt->work_next, 1u);
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(32 * kPrecWarps) k_refine_fp32(RefineArgs a) {
                     }
                 }
                 enqueue(a, Q, qn, hit, pw, prio_pack(0, p1, 0, j), sFx[i], sFy[i], hit ? sFx[j] : 0.f,
-                        hit ? sFy[j] : 0.f);
+                        hit ? sFy[j] : 0.f, tag);
             }
         }
         /* cross-leaf checks that target this leaf: p1 = the querier */
@@ -135,12 +136,12 @@ __global__ void __launch_bounds__(32 * kPrecWarps) k_refine_fp32(RefineArgs a) {
                     }
                 }
                 enqueue(a, Q, qn, hit, pw, prio_pack(1, q, qe.y, j), qf.x, qf.y, hit ? sFx[j] : 0.f,
-                        hit ? sFy[j] : 0.f);
+                        hit ? sFy[j] : 0.f, tag);
             }
         }
         __syncwarp();
     }
-    drain_queue(a, Q, qn);
+    drain_queue(a, Q, qn, tag);
     for (int o = 16; o > 0; o >>= 1) {
         cand += __shfl_down_sync(0xffffffffu, cand, o);
         hits += __shfl_down_sync(0xffffffffu, hits, o);

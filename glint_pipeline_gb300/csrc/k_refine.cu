@@ -45,6 +45,7 @@ __global__ void __launch_bounds__(32 * kRefineWarps) k_refine_fp64(RefineArgs a)
     unsigned long long cand = 0, hits = 0;
     uint32_t qn = 0;
     const uint32_t nwork = a.cnt->n_leaf_work;
+    const uint32_t tag = a.cnt->step_tag;
     for (;;) {
         uint32_t li = 0;
         if (lane == 0) li = atomicAdd(&a.cnt->work_next, 1u);
@@ -83,7 +84,7 @@ __global__ void __launch_bounds__(32 * kRefineWarps) k_refine_fp64(RefineArgs a)
                         fy2 = (float)y2;
                     }
                 }
-                enqueue(a, Q, qn, hit, pw, prio_pack(0, p1, 0, j), fx1, fy1, fx2, fy2);
+                enqueue(a, Q, qn, hit, pw, prio_pack(0, p1, 0, j), fx1, fy1, fx2, fy2, tag);
             }
         }
         /* cross-leaf checks that target this leaf */
@@ -120,12 +121,12 @@ __global__ void __launch_bounds__(32 * kRefineWarps) k_refine_fp64(RefineArgs a)
                         }
                     }
                 }
-                enqueue(a, Q, qn, hit, pw, prio_pack(1, q, qe.y, j), fqx, fqy, fx2, fy2);
+                enqueue(a, Q, qn, hit, pw, prio_pack(1, q, qe.y, j), fqx, fqy, fx2, fy2, tag);
             }
         }
         __syncwarp();
     }
-    drain_queue(a, Q, qn);
+    drain_queue(a, Q, qn, tag);
     for (int o = 16; o > 0; o >>= 1) {
         cand += __shfl_down_sync(0xffffffffu, cand, o);
         hits += __shfl_down_sync(0xffffffffu, hits, o);
@@ -166,7 +167,6 @@ RefineArgs refine_args(glint_ctx *c) {
     a.Bm = c->Bm;
     a.new_cap = c->new_cap;
     a.cap = c->cap;
-    a.st = stamp_of(c->step_index);
     a.ex = make_exact(c);
     a.cnt = c->d_cnt;
     return a;
@@ -216,10 +216,11 @@ __device__ inline void touch_box(TRec &r, const float2 &A, const float2 &Bp) {
 
 __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ list, TRec *tab, uint8_t *stamp,
                                                 uint64_t B, uint64_t Bm, uint64_t new_cap,
-                                                const float2 *__restrict__ fpos, uint32_t N, uint8_t st,
+                                                const float2 *__restrict__ fpos, uint32_t N,
                                                 DevCounters *cnt) {
     const unsigned long long n0 = cnt->new_keys;
     const unsigned long long n = n0 < new_cap ? n0 : new_cap;
+    const uint8_t st = (uint8_t)cnt->step_tag;
     for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < n;
          i += (unsigned long long)gridDim.x * blockDim.x) {
         ulonglong2 cur = make_ulonglong2(list[i].key | kNewFlag, list[i].prio);
@@ -278,10 +279,9 @@ __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ lis
 }
 
 cudaError_t launch_insert(glint_ctx *c, uint32_t cur_time) {
-    const uint8_t st = stamp_of(c->step_index);
     (void)cur_time;
     k_insert<<<152 * 8, 256, 0, c->stream>>>(c->d_new, c->d_tab, c->d_stamp, c->B, c->Bm, c->new_cap, c->d_fpos, c->N,
-                                             st, c->d_cnt);
+                                             c->d_cnt);
     return cudaGetLastError();
 }
 

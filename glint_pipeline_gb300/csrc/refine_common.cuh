@@ -40,7 +40,6 @@ struct RefineArgs {
     NewEntry *newlist;
     uint64_t B, Bm, new_cap;
     uint32_t cap;
-    uint8_t st;
     Frame f;
     ExactCtx ex;
     DevCounters *cnt;
@@ -50,7 +49,7 @@ struct RefineArgs {
  * the refine kernels run.  Found -> touch the entry (tag, f32 box; each pair
  * has at most one event per step, so the box needs no atomics).  Not found
  * before an empty slot -> the pair is new this step. */
-__device__ inline bool table_touch(const RefineArgs &a, const QEntry &q) {
+__device__ inline bool table_touch(const RefineArgs &a, const QEntry &q, uint32_t tag) {
     uint64_t slot = fastmod(cantor(pair_a(q.pw), pair_b(q.pw)), a.B, a.Bm);
     for (uint32_t probe = 0; probe < kProbeLimit; ++probe) {
         const unsigned long long w0 = a.tab[slot].w0;
@@ -65,7 +64,7 @@ __device__ inline bool table_touch(const RefineArgs &a, const QEntry &q) {
                 m.w = max(m.w, hy);
                 *reinterpret_cast<uint4 *>(a.tab[slot].mbr) = m;
             }
-            rec_set_tag(a.tab[slot], a.st);
+            rec_set_tag(a.tab[slot], tag);
             return false;
         }
         if (w0 == kEmptyW0) return true;
@@ -76,7 +75,7 @@ __device__ inline bool table_touch(const RefineArgs &a, const QEntry &q) {
 }
 
 /* warp-collective: process queue entries [0, n) one per lane */
-__device__ inline void drain_queue(const RefineArgs &a, QEntry *Q, uint32_t n) {
+__device__ inline void drain_queue(const RefineArgs &a, QEntry *Q, uint32_t n, uint32_t tag) {
     const int lane = threadIdx.x & 31;
     for (uint32_t base = 0; base < n; base += 32) {
         const uint32_t e = base + lane;
@@ -84,7 +83,7 @@ __device__ inline void drain_queue(const RefineArgs &a, QEntry *Q, uint32_t n) {
         QEntry q;
         if (e < n) {
             q = Q[e];
-            isnew = table_touch(a, q);
+            isnew = table_touch(a, q, tag);
         }
         const unsigned m = __ballot_sync(0xffffffffu, isnew);
         if (m) {
@@ -108,7 +107,7 @@ __device__ inline void drain_queue(const RefineArgs &a, QEntry *Q, uint32_t n) {
 
 /* warp-collective: append this lane's contact (if any) to the queue */
 __device__ inline void enqueue(const RefineArgs &a, QEntry *Q, uint32_t &qn, bool hit, unsigned long long pw,
-                               unsigned long long prio, float x1, float y1, float x2, float y2) {
+                               unsigned long long prio, float x1, float y1, float x2, float y2, uint32_t tag) {
     const int lane = threadIdx.x & 31;
     const unsigned m = __ballot_sync(0xffffffffu, hit);
     if (hit) {
@@ -123,7 +122,7 @@ __device__ inline void enqueue(const RefineArgs &a, QEntry *Q, uint32_t &qn, boo
     qn += __popc(m);
     __syncwarp();
     if (qn >= 32) {
-        drain_queue(a, Q, 32);
+        drain_queue(a, Q, 32, tag);
         const uint32_t rest = qn - 32;
         if ((uint32_t)lane < rest) Q[lane] = Q[32 + lane];
         __syncwarp();

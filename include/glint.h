@@ -95,6 +95,9 @@ typedef struct glint_config {
     uint64_t kv_restriction;       /* 0 -> G_bytes*2^25 keys (util/config.h:80) */
     uint64_t kv_capacity;          /* key buffer; 0 -> kv_restriction + max(1000000, 4*num_objects)
                                       (util/config.h:81 adds 1000000) */
+    uint32_t use_graph;            /* 1: capture the step once as a CUDA graph and replay it (device
+                                      input buffer only; per-stage timing off) */
+    uint32_t reserved2;
 } glint_config;
 
 typedef struct glint_box {

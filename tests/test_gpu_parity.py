@@ -214,3 +214,34 @@ def _cudart():
         except OSError:
             continue
     raise OSError("libcudart not found")
+
+
+def test_graph_mode_parity():
+    """The step captured once as a CUDA graph and replayed from a fixed device
+    input buffer gives the oracle's meetings, counts and state."""
+    import ctypes
+    name = "dense_20k"
+    box, pts = make_points(name, 40)
+    cfgd = case_config(name)
+    o = Oracle(make_config(**cfgd), box, pts[0])
+    g = DeviceBench(gpu_config(cfgd, use_graph=True, precision_mode=1), box, pts[0])
+    rt = _cudart()
+    n = cfgd["num_objects"]
+    buf = ctypes.c_void_p()
+    assert rt.cudaMalloc(ctypes.byref(buf), ctypes.c_size_t(16 * n)) == 0
+    try:
+        for t in range(pts.shape[0]):
+            o.step(pts[t], t)
+            host = np.ascontiguousarray(pts[t])
+            assert rt.cudaMemcpy(buf, host.ctypes.data_as(ctypes.c_void_p), ctypes.c_size_t(16 * n), 1) == 0
+            g.step_device(buf.value, t)
+            st = g.sync()
+            c = o.counts()
+            assert st.error_flags & ~EF_INFO == 0
+            assert (st.checks, st.candidates, st.contacts) == (c.grid_check_counter, c.candidates, c.contacts), t
+            compare_meetings(o.meetings(), g.meetings(), t)
+        compare_state(o, g)
+    finally:
+        rt.cudaFree(buf)
+        g.close()
+        o.close()
