@@ -264,9 +264,24 @@ class DeviceBench:
     def last_error(self) -> str:
         return self.lib.glint_last_error(self.h).decode()
 
+    @classmethod
+    def _view(cls, handle: int, config: Configuration):
+        """A DeviceBench over a context owned elsewhere (a batch region)."""
+        b = cls.__new__(cls)
+        b.lib = _abi.lib()
+        b.config = config
+        b.n = int(config.num_objects)
+        b.h = ctypes.c_void_p(handle)
+        b._owned = False
+        sc, gc, bk = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint64()
+        b.lib.glint_get_capacities(b.h, ctypes.byref(sc), ctypes.byref(gc), ctypes.byref(bk))
+        b.schema_capacity, b.grids_capacity, b.num_buckets = sc.value, gc.value, bk.value
+        return b
+
     def close(self):
         if getattr(self, "h", None):
-            self.lib.glint_destroy(self.h)
+            if getattr(self, "_owned", True):
+                self.lib.glint_destroy(self.h)
             self.h = None
 
     def __del__(self):

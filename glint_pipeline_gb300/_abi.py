@@ -197,6 +197,14 @@ def load_library(path: str | None = None):
     lib.glint_server_poll.argtypes = [vp, u64, ctypes.POINTER(GlintQueryResult), ctypes.POINTER(ctypes.c_int)]
     lib.glint_store_read.argtypes = [vp] * 9 + [ctypes.POINTER(GlintStoreInfo)]
     lib.glint_active_search_noalloc.argtypes = [vp, vp, u32, vp, u64, vp]
+    lib.glint_batch_create.argtypes = [u32, vp, vp, vp, ctypes.POINTER(vp)]
+    lib.glint_batch_destroy.argtypes = [vp]
+    lib.glint_batch_regions.restype = u32
+    lib.glint_batch_regions.argtypes = [vp]
+    lib.glint_batch_region.restype = vp
+    lib.glint_batch_region.argtypes = [vp, u32]
+    lib.glint_batch_step.argtypes = [vp, vp, u32]
+    lib.glint_batch_sync.argtypes = [vp, vp]
     lib.glint_gen_create.argtypes = [vp, u32, vp, u32, u32, u32, ctypes.POINTER(vp)]
     lib.glint_gen_step.argtypes = [vp, vp, vp]
     lib.glint_gen_destroy.argtypes = [vp]

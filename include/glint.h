@@ -361,6 +361,24 @@ glint_status glint_active_search(glint_ctx *ctx, const uint32_t *pids, uint32_t 
 glint_status glint_active_search_noalloc(glint_ctx *ctx, const uint32_t *d_pids, uint32_t npids,
                                          glint_search_info *d_out, uint64_t cap, uint64_t *d_n);
 
+/* ---- batching form: many independent regions on one GPU ------------------
+ * Each region is a context created from cfgs[r] (its step captured as a CUDA
+ * graph, per-stage timing off) with its own stream.  glint_batch_step
+ * launches every region's step for cur_time, reading d_points[r] (device
+ * memory; keep the same buffer per region so the captured graph is reused),
+ * and returns without waiting; glint_batch_sync waits for all of them and
+ * runs each region's automatic flush, filling stats[r] when stats is not
+ * NULL.  glint_batch_region gives a region's context for its meetings,
+ * store and queries. */
+typedef struct glint_batch glint_batch;
+glint_status glint_batch_create(uint32_t num_regions, const glint_config *cfgs, const glint_box *mbrs,
+                                const double *const *first_points, glint_batch **out);
+glint_status glint_batch_destroy(glint_batch *batch);
+uint32_t glint_batch_regions(const glint_batch *batch);
+glint_ctx *glint_batch_region(glint_batch *batch, uint32_t region);
+glint_status glint_batch_step(glint_batch *batch, const double *const *d_points, uint32_t cur_time);
+glint_status glint_batch_sync(glint_batch *batch, glint_step_stats *stats);
+
 /* ---- synthetic trajectories on the device (benchmark input) ----
  * params/objects: the generator's parameter block and object states as
  * produced by the host generator (glint_pipeline_gb300/csrc/tracegen.h) */
