@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=6.0)
     p.add_argument("--serve-rate", type=float, default=200.0)
     p.add_argument("--no-serve", action="store_true")
+    p.add_argument("--workload", default="step10m", choices=["step10m", "batch64", "skew50m"],
+                   help="step10m: the headline line; batch64 / skew50m: the batching and precision forms")
+    p.add_argument("--regions", type=int, default=64)
     return p.parse_args()
 
 
@@ -426,11 +429,163 @@ def serving(args, bench, N, t_hi):
                                  "queries": len(two)}}
 
 
+def next_pow2(v):
+    p = 1
+    while p < v:
+        p <<= 1
+    return p
+
+
+def run_batch(args, local):
+    """Batching form: R regions, populations log-uniform in [1k, 2M], each with
+    its own generator seed, street grid and hotspots, advanced together
+    (glint_batch_*: per-region streams, captured step graphs) against the
+    same regions stepped one after another without graphs; an autotuner picks
+    leaf capacity and hash load factor per size class for a tuned run."""
+    import glint_pipeline_gb300 as gp
+    from glint_pipeline_gb300 import _abi
+    from glint_pipeline_gb300.batch import Batch, autotune
+    from glint_pipeline_gb300.tracegen import SEED_REGIONS, TraceGenerator
+    lib = _abi.lib()
+    rt = cudart()
+    rt.cudaSetDevice(local)
+    R = args.regions
+    rng = np.random.default_rng(SEED_REGIONS)
+    pops = np.exp(rng.uniform(np.log(1_000), np.log(2_000_000), R)).astype(np.int64)
+    K, W = args.steps, max(args.warmup, 3)
+    total = W + K
+    regions = []
+    for r in range(R):
+        n = int(pops[r])
+        ext = float(np.clip(40000.0 * np.sqrt(n / 10_000_000), 2000.0, 40000.0))
+        g = TraceGenerator(SEED_REGIONS ^ (r + 1), n, 0, extent_m=ext)
+        g2 = TraceGenerator(SEED_REGIONS ^ (r + 1), n, 0, extent_m=ext)
+        box, first = g.box(), g.steps(1)[0]
+        pb, ob = g2.params_bytes(), g2.objects_bytes()
+        buf = ctypes.c_void_p()
+        assert rt.cudaMalloc(ctypes.byref(buf), ctypes.c_size_t(16 * n * total)) == 0
+        gh = ctypes.c_void_p()
+        assert lib.glint_gen_create(pb, len(pb), ob, n, len(ob) // n, 0, ctypes.byref(gh)) == 0
+        for t in range(total):
+            lib.glint_gen_step(gh, ctypes.c_void_p(buf.value + 16 * n * t), None)
+        rt.cudaDeviceSynchronize()
+        lib.glint_gen_destroy(gh)
+        inp = ctypes.c_void_p()
+        assert rt.cudaMalloc(ctypes.byref(inp), ctypes.c_size_t(16 * n)) == 0
+        regions.append({"n": n, "box": box, "first": first, "steps": buf, "input": inp})
+
+    def config(n, cap=50, lf=None):
+        b = next_pow2(int(64 * n)) if lf is None else next_pow2(int(28 * n / lf))
+        return gp.Configuration(num_objects=n, num_meeting_buckets=b, grid_capacity=cap, precision_mode=1,
+                                auto_flush=True, kv_restriction=max(1 << 20, 8 * n), store_keep=2, device=local)
+
+    def copy_in(t, streams):
+        for r, reg in enumerate(regions):
+            rt.cudaMemcpyAsync(reg["input"], ctypes.c_void_p(reg["steps"].value + 16 * reg["n"] * t),
+                               ctypes.c_size_t(16 * reg["n"]), 3, ctypes.c_void_p(streams[r]))
+
+    def batched(cfgs):
+        batch = Batch(cfgs, [x["box"] for x in regions], [x["first"] for x in regions])
+        streams = [batch.stream(r) for r in range(R)]
+        ptrs = [x["input"].value for x in regions]
+        for t in range(W):
+            copy_in(t, streams)
+            batch.step(ptrs, t)
+            batch.sync()
+        rt.cudaDeviceSynchronize()
+        with Clocks(local, "batch") as clk:
+            t0 = time.perf_counter()
+            for t in range(W, total):
+                copy_in(t, streams)
+                batch.step(ptrs, t)
+                batch.sync()
+            rt.cudaDeviceSynchronize()
+            dt = time.perf_counter() - t0
+        batch.close()
+        return dt, clk.summary()
+
+    def sequential(cfgs):
+        benches = [gp.DeviceBench(c, x["box"], x["first"]) for c, x in zip(cfgs, regions)]
+        for t in range(W):
+            for b, x in zip(benches, regions):
+                b.step_device(x["steps"].value + 16 * x["n"] * t, t)
+                b.sync()
+        rt.cudaDeviceSynchronize()
+        t0 = time.perf_counter()
+        for t in range(W, total):
+            for b, x in zip(benches, regions):
+                b.step_device(x["steps"].value + 16 * x["n"] * t, t)
+                b.sync()
+        rt.cudaDeviceSynchronize()
+        dt = time.perf_counter() - t0
+        for b in benches:
+            b.close()
+        return dt
+
+    objs = int(pops.sum())
+    default_cfgs = [config(x["n"]) for x in regions]
+    t_batch, clk = batched(default_cfgs)
+    t_seq = sequential(default_cfgs)
+    # autotune one representative region per size class
+    classes = [(0, 10_000), (10_000, 100_000), (100_000, 1_000_000), (1_000_000, 1 << 40)]
+    picks, tables = {}, {}
+    for lo, hi in classes:
+        members = [r for r in range(R) if lo <= regions[r]["n"] < hi]
+        if not members:
+            continue
+        rep = regions[members[len(members) // 2]]
+
+        def trial(cfg, rep=rep):
+            b = gp.DeviceBench(cfg, rep["box"], rep["first"])
+            for t in range(3):
+                b.step_device(rep["steps"].value + 16 * rep["n"] * t, t)
+                b.sync()
+            rt.cudaDeviceSynchronize()
+            t0 = time.perf_counter()
+            for t in range(3, 6):
+                b.step_device(rep["steps"].value + 16 * rep["n"] * t, t)
+                b.sync()
+            dt = (time.perf_counter() - t0) / 3
+            b.close()
+            return dt
+        best, table = autotune(lambda cap, lf, n=rep["n"]: config(n, cap, lf), trial,
+                               capacities=(32, 50, 128, 512), load_factors=(0.5, 0.9))
+        picks[f"{lo}-{hi}"] = {"capacity": best[0], "load_factor": best[1]}
+        tables[f"{lo}-{hi}"] = table
+    tuned_cfgs = []
+    for x in regions:
+        key = next(f"{lo}-{hi}" for lo, hi in classes if lo <= x["n"] < hi)
+        p = picks[key]
+        tuned_cfgs.append(config(x["n"], p["capacity"], p["load_factor"]))
+    t_tuned, _ = batched(tuned_cfgs)
+    for x in regions:
+        rt.cudaFree(x["steps"])
+        rt.cudaFree(x["input"])
+    line = {"metric": "object-timesteps/s, 64 independent regions on one GPU (batching form)",
+            "value": objs * K / t_batch, "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": W,
+            "ms_per_step": 1000.0 * t_batch / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"{R} regions, populations log-uniform in [1k, 2M] ({objs} objects), own street "
+                                   f"grid, seed and hotspots each; reach 2 m, min meeting 5",
+                       "regions": R, "objects": objs, "timing": "host wall clock around each batch step and sync"},
+            "clocks": clk,
+            "forms": {"batched_graphs": {"value": objs * K / t_batch, "ms_per_step": 1000.0 * t_batch / K},
+                      "sequential_no_graph": {"value": objs * K / t_seq, "ms_per_step": 1000.0 * t_seq / K},
+                      "batched_autotuned": {"value": objs * K / t_tuned, "ms_per_step": 1000.0 * t_tuned / K,
+                                            "picks": picks}},
+            "speedup_batched_vs_sequential": t_seq / t_batch, "autotune": tables}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_init()
     if args.impl == "reference":
         run_reference_arm(args, rank, world, pg)
+        return
+    if args.workload == "batch64":
+        if rank == 0:
+            run_batch(args, local)
         return
     from glint_pipeline_gb300 import _abi
     from glint_pipeline_gb300.tracegen import SEED_SCALE, TraceGenerator
