@@ -65,6 +65,9 @@ def parse():
     p.add_argument("--workload", default="step10m", choices=["step10m", "batch64", "skew50m"],
                    help="step10m: the headline line; batch64 / skew50m: the batching and precision forms")
     p.add_argument("--regions", type=int, default=64)
+    p.add_argument("--skew-objects", type=int, default=50_000_000)
+    p.add_argument("--skew-buckets", type=int, default=1 << 31)
+    p.add_argument("--core-objects", type=int, default=2_000_000)
     return p.parse_args()
 
 
@@ -577,6 +580,119 @@ def run_batch(args, local):
     print(json.dumps(line), flush=True)
 
 
+def meeting_digest(m):
+    """Order-sensitive 64-bit digest of a meeting list (records compared in
+    the order the step reported them)."""
+    w = np.ascontiguousarray(m).view(np.uint64).ravel()
+    h = np.uint64(w.size)
+    chunk = 1 << 24
+    with np.errstate(over="ignore"):
+        for s in range(0, w.size, chunk):
+            x = w[s:s + chunk]
+            k = np.arange(2 * s + 1, 2 * (s + x.size) + 1, 2, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15)
+            y = (x ^ (x >> np.uint64(29))) * np.uint64(0xBF58476D1CE4E5B9)
+            h = h + (y * k).sum(dtype=np.uint64)
+    return int(h)
+
+
+# the 1%-area skew: 5 hotspots whose 2-sigma discs cover 1% of the 40x40 km box
+SKEW_SIGMA_SPREAD = float(np.sqrt(0.01 * 40000.0 ** 2 / (5 * np.pi)) / 2)
+
+
+def run_skew(args, local):
+    """Precision form on extreme skew: 20% of the objects start at 5 hotspots,
+    the rest uniform over the 40x40 km street grid.  Two cases: 'spread'
+    (50M objects, hotspots covering 1% of the area) for throughput, and 'core'
+    (hotspots with sigma 50 m, 2M objects; at 50M objects that shape puts
+    ~8e10 contacts in one step, beyond any meeting table) for the densest
+    contacts.  Each case runs the plain FP64 refine and the FP32 guard-band
+    refine on the same device-generated trajectories; every step's meeting
+    list is compared between the two (order-sensitive digest), the band hit
+    rate is the refine's in-band pairs over its distance tests, and
+    glint_precision_probe gives max |d32 - d64| on sampled pairs."""
+    import glint_pipeline_gb300 as gp
+    from glint_pipeline_gb300 import _abi
+    from glint_pipeline_gb300.tracegen import SEED_SKEW, TraceGenerator
+    lib = _abi.lib()
+    rt = cudart()
+    rt.cudaSetDevice(local)
+    K, W = args.steps, max(args.warmup, 3)
+    cases = [("spread", args.skew_objects, SKEW_SIGMA_SPREAD, args.skew_buckets, 256),
+             ("core", args.core_objects, 50.0, next_pow2(256 * args.core_objects), 16)]
+    out = {}
+    for name, N, sigma, B, stride in cases:
+        gen = TraceGenerator(SEED_SKEW, N, 1, sigma_m=sigma)
+        pb, ob = gen.params_bytes(), gen.objects_bytes()  # the state before step 0
+        box, first = gen.box(), gen.steps(1)[0]
+        gen.close()
+        res = {}
+        for mode in ("plain", "tuned"):
+            cfg = gp.Configuration(num_objects=N, num_meeting_buckets=B, device=local, timing=True,
+                                   precision_mode=1 if mode == "tuned" else 0, auto_flush=True, store_keep=1,
+                                   meeting_log_capacity=max(1 << 24, 4 * N))
+            bench = gp.DeviceBench(cfg, box, first)
+            gh = ctypes.c_void_p()
+            assert lib.glint_gen_create(pb, len(pb), ob, N, len(ob) // N, 0, ctypes.byref(gh)) == 0
+            buf = ctypes.c_void_p()
+            assert rt.cudaMalloc(ctypes.byref(buf), ctypes.c_size_t(16 * N)) == 0
+            digests, counts = [], []
+            stage_ms = np.zeros(8)
+            dev_ms, flush_ms, launches, flags = 0.0, 0.0, 0, 0
+            acc = {"candidates": 0, "contacts": 0, "band_pairs": 0, "box_band": 0, "new_keys": 0, "meetings": 0}
+            with Clocks(local, f"skew_{name}_{mode}") as clk:
+                for t in range(W + K):
+                    lib.glint_gen_step(gh, buf, ctypes.c_void_p(bench.stream))
+                    bench.step_device(buf.value, t)
+                    st = bench.sync()
+                    flags |= st.error_flags
+                    if t >= W:
+                        stage_ms += np.array(st.ms)
+                        dev_ms += st.ms[7] + st.flush_ms
+                        flush_ms += st.flush_ms
+                        launches += st.launches
+                        for k in acc:
+                            acc[k] += getattr(st, k)
+                    m = bench.meetings()
+                    digests.append(meeting_digest(m))
+                    counts.append(int(m.shape[0]))
+                    del m
+            probe = bench.precision_probe(stride)
+            lib.glint_gen_destroy(gh)
+            rt.cudaFree(buf)
+            bench.close()
+            stage = {k: v / K for k, v in zip(STAGES, stage_ms)}
+            stage["flush"] = flush_ms / K
+            stage["total"] += stage["flush"]
+            res[mode] = {"value": N * K / (dev_ms / 1000.0), "ms_per_step": dev_ms / K, "stage_ms": stage,
+                         "per_step": {k: v / K for k, v in acc.items()}, "error_flags": flags,
+                         "gpu_launches": launches, "clocks": clk.summary(), "probe": probe,
+                         "_digests": digests, "meetings_per_step": counts}
+        dp, dt = res["plain"].pop("_digests"), res["tuned"].pop("_digests")
+        steps_differ = [t for t in range(len(dp)) if dp[t] != dt[t] or
+                        res["plain"]["meetings_per_step"][t] != res["tuned"]["meetings_per_step"][t]]
+        tu = res["tuned"]["per_step"]
+        out[name] = {"objects": N, "sigma_m": sigma, "buckets": B, "forms": res,
+                     "meetings_compared": int(sum(res["plain"]["meetings_per_step"])),
+                     "steps_compared": len(dp), "steps_differing": steps_differ,
+                     "band_hit_rate": tu["band_pairs"] / max(tu["candidates"], 1),
+                     "box_band_per_step": tu["box_band"],
+                     "speedup_tuned_vs_plain": res["plain"]["ms_per_step"] / res["tuned"]["ms_per_step"]}
+    sp = out["spread"]
+    head = sp["forms"]["tuned"]
+    line = {"metric": "object-timesteps/s, precision form (FP32 guard band) on extreme skew, meetings equal to "
+                      "the FP64 form",
+            "value": head["value"], "unit": UNIT, "n_gpus": 1, "steps": K, "warmup": W,
+            "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64+f32", "data": "synthetic",
+            "config": {"workload": f"Manhattan-grid generator, 40x40 km: {sp['objects']} objects, 20% at 5 "
+                                   f"hotspots (sigma {SKEW_SIGMA_SPREAD:.0f} m: 1% of the area), reach 2 m, "
+                                   f"min meeting 5, {sp['buckets']} buckets; plus a sigma 50 m core case of "
+                                   f"{out['core']['objects']} objects",
+                       "l2": "inputs larger than L2"},
+            "clocks": head["clocks"], "gpu_launches": head["gpu_launches"], "cases": out}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_init()
@@ -586,6 +702,10 @@ def main():
     if args.workload == "batch64":
         if rank == 0:
             run_batch(args, local)
+        return
+    if args.workload == "skew50m":
+        if rank == 0:
+            run_skew(args, local)
         return
     from glint_pipeline_gb300 import _abi
     from glint_pipeline_gb300.tracegen import SEED_SCALE, TraceGenerator

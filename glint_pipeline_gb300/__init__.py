@@ -165,6 +165,16 @@ class DeviceBench:
             raise GlintError(st, self.last_error())
         return out[: min(int(n.value), int(cap))]
 
+    def precision_probe(self, stride: int = 256) -> dict:
+        """The FP32 screen of the precision form against the reference's FP64
+        distance test on pairs sampled from the last step (every stride-th
+        object of the leaf-major order with its 32 successors)."""
+        rep = _abi.GlintPrecisionReport()
+        st = self.lib.glint_precision_probe(self.h, int(stride), ctypes.byref(rep))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        return rep.as_dict()
+
     # -- key-value store -----------------------------------------------------
     def flush(self) -> "_abi.GlintStoreInfo":
         """Flush the pending keys into the store now (cuda/geometry.cu:1752-2135)."""

@@ -151,6 +151,16 @@ class GlintQueryResult(ctypes.Structure):
                 ("hop_end", ctypes.c_uint64 * 8), ("keys_scanned", ctypes.c_uint64)]
 
 
+class GlintPrecisionReport(ctypes.Structure):
+    _fields_ = [("pairs", ctypes.c_uint64), ("in_band", ctypes.c_uint64), ("mismatches", ctypes.c_uint64),
+                ("contacts", ctypes.c_uint64), ("max_abs_err_m", ctypes.c_double),
+                ("max_abs_err_near_m", ctypes.c_double), ("max_band_m", ctypes.c_double),
+                ("stride", ctypes.c_uint32), ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 # glint_search_info = search_info_unit (tracing/workbench.h:85-88)
 SEARCH_DTYPE = np.dtype([("pid", "<u4"), ("target", "<u4"), ("start", "<u4"), ("end", "<u4"), ("mbr", "<f4", (4,))])
 assert SEARCH_DTYPE.itemsize == 32
@@ -197,6 +207,7 @@ def load_library(path: str | None = None):
     lib.glint_server_poll.argtypes = [vp, u64, ctypes.POINTER(GlintQueryResult), ctypes.POINTER(ctypes.c_int)]
     lib.glint_store_read.argtypes = [vp] * 9 + [ctypes.POINTER(GlintStoreInfo)]
     lib.glint_active_search_noalloc.argtypes = [vp, vp, u32, vp, u64, vp]
+    lib.glint_precision_probe.argtypes = [vp, u32, ctypes.POINTER(GlintPrecisionReport)]
     lib.glint_batch_create.argtypes = [u32, vp, vp, vp, ctypes.POINTER(vp)]
     lib.glint_batch_destroy.argtypes = [vp]
     lib.glint_batch_regions.restype = u32

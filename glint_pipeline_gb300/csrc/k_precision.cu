@@ -12,6 +12,8 @@
  * object's cx = 1/(L(y1) S).  No FP64 instruction runs per pair outside the
  * band: on sm_103a FP64 issues at a small fraction of the FP32 rate.
  */
+#include <cstring>
+
 #include "refine_common.cuh"
 
 namespace glint {
@@ -169,4 +171,125 @@ void refine_prec_set_attributes(uint32_t cap) {
                          (int)refine_prec_smem_bytes(cap));
 }
 
+/* ---- probe: the screen against the FP64 test on sampled pairs --------------
+ * Pairs (i, i + o), o = 1..32, for leaf-major ranks i = 0, stride, 2 stride,
+ * ...: neighbours in that order share a leaf or sit in adjacent leaves, so the
+ * sample is dominated by short distances, where the decision is made. */
+struct ProbeAcc {
+    unsigned long long pairs, in_band, mismatches, contacts;
+    unsigned long long err_bits, err_near_bits, band_bits; /* non-negative doubles as bits */
+};
+
+__device__ inline unsigned long long warp_sum(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ inline unsigned long long warp_max(unsigned long long v) {
+    for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long w = __shfl_down_sync(0xffffffffu, v, o);
+        v = w > v ? w : v;
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(256) k_precision_probe(const longlong2 *__restrict__ sipos,
+                                                         const double2 *__restrict__ sxy,
+                                                         const float *__restrict__ sc, uint32_t N, uint32_t stride,
+                                                         Frame f, ExactCtx ex, ProbeAcc *acc) {
+    const unsigned long long samples = ((unsigned long long)N + stride - 1) / stride;
+    const unsigned long long total = samples * 32;
+    unsigned long long pairs = 0, band = 0, mism = 0, hits = 0;
+    double err = 0.0, err_near = 0.0, bandm = 0.0;
+    const double r = ex.r;
+    const unsigned long long step = (unsigned long long)gridDim.x * blockDim.x;
+    /* every lane runs the same number of iterations (the warp reductions
+     * below need all 32) */
+    const unsigned long long start = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x;
+    for (unsigned long long it0 = start - (threadIdx.x & 31); it0 < total; it0 += step) {
+        const unsigned long long it = it0 + (threadIdx.x & 31);
+        const unsigned long long i = (it >> 5) * stride, j = i + (it & 31) + 1;
+        if (it >= total || j >= N) continue;
+        ++pairs;
+        const longlong2 a = sipos[i], b = sipos[j];
+        const float ci = sc[i], cj = sc[j];
+        const long long dx = a.x - b.x, dy = a.y - b.y;
+        const Screen s = make_screen(__fmaf_rn(0.0f, cj, ci), f);
+        const int scr = fx_screen(dx, dy, s, f.cy);
+        const double2 P = sxy[i], Q = sxy[j];
+        const bool within = point_le_exact(P.x, P.y, Q.x, Q.y, dpm_lon_fast(P.y), ex);
+        hits += within ? 1 : 0;
+        if (scr < 0) ++band;
+        else if ((scr == 1) != within) ++mism;
+        const float mx = fx_to_f(dx) * s.cx, my = fx_to_f(dy) * f.cy;
+        const float d32 = sqrtf(mx * mx + my * my);
+        if (d32 == d32) {
+            const double d64 = point_dist(P.x, P.y, Q.x, Q.y, dpm_lon_fast(P.y), ex.dpm_lat);
+            const double e = fabs((double)d32 - d64);
+            err = fmax(err, e);
+            if (d64 <= 2.0 * r) err_near = fmax(err_near, e);
+            const double bw = (double)(f.band0 + f.band1 * (s.cx + f.cy)) / (2.0 * r);
+            if (bw == bw) bandm = fmax(bandm, bw);
+        }
+    }
+    pairs = warp_sum(pairs);
+    band = warp_sum(band);
+    mism = warp_sum(mism);
+    hits = warp_sum(hits);
+    const unsigned long long eb = warp_max((unsigned long long)__double_as_longlong(err));
+    const unsigned long long enb = warp_max((unsigned long long)__double_as_longlong(err_near));
+    const unsigned long long bb = warp_max((unsigned long long)__double_as_longlong(bandm));
+    if ((threadIdx.x & 31) == 0 && pairs) {
+        atomicAdd(&acc->pairs, pairs);
+        atomicAdd(&acc->in_band, band);
+        atomicAdd(&acc->mismatches, mism);
+        atomicAdd(&acc->contacts, hits);
+        atomicMax(&acc->err_bits, eb);
+        atomicMax(&acc->err_near_bits, enb);
+        atomicMax(&acc->band_bits, bb);
+    }
+}
+
 } // namespace glint
+
+using namespace glint;
+
+extern "C" glint_status glint_precision_probe(glint_ctx *c, uint32_t stride, glint_precision_report *out) {
+    if (!c || !out || stride == 0) return GLINT_ERR_INVALID_ARGUMENT;
+    if (c->step_index == 0) {
+        c->last_error = "precision probe before the first step";
+        return GLINT_ERR_STATE;
+    }
+    cudaSetDevice(c->device);
+    ProbeAcc *d = nullptr;
+    ProbeAcc h;
+    std::memset(&h, 0, sizeof(h));
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&d, sizeof(ProbeAcc));
+    if (e == cudaSuccess) e = cudaMemsetAsync(d, 0, sizeof(ProbeAcc), c->stream);
+    if (e == cudaSuccess) {
+        ExactCtx ex = make_exact(c);
+        ex.ambiguous = nullptr; /* the step's counters stay the step's */
+        ex.rechecks = nullptr;
+        const unsigned long long total = (((unsigned long long)c->N + stride - 1) / stride) * 32;
+        k_precision_probe<<<grid_for(total, 256, 152u * 8u), 256, 0, c->stream>>>(c->d_sipos, c->d_sxy, c->d_sc,
+                                                                                 c->N, stride, c->frame, ex, d);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d, sizeof(h), cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (d) cudaFree(d);
+    if (e != cudaSuccess) {
+        c->last_error = std::string("precision probe: ") + cudaGetErrorString(e);
+        return e == cudaErrorMemoryAllocation ? GLINT_ERR_OUT_OF_MEMORY : GLINT_ERR_CUDA;
+    }
+    std::memset(out, 0, sizeof(*out));
+    out->pairs = h.pairs;
+    out->in_band = h.in_band;
+    out->mismatches = h.mismatches;
+    out->contacts = h.contacts;
+    std::memcpy(&out->max_abs_err_m, &h.err_bits, sizeof(double));
+    std::memcpy(&out->max_abs_err_near_m, &h.err_near_bits, sizeof(double));
+    std::memcpy(&out->max_band_m, &h.band_bits, sizeof(double));
+    out->stride = stride;
+    return GLINT_OK;
+}

@@ -361,6 +361,30 @@ glint_status glint_active_search(glint_ctx *ctx, const uint32_t *pids, uint32_t 
 glint_status glint_active_search_noalloc(glint_ctx *ctx, const uint32_t *d_pids, uint32_t npids,
                                          glint_search_info *d_out, uint64_t cap, uint64_t *d_n);
 
+/* ---- precision form: the FP32 screen against the FP64 test ---------------
+ * No counterpart in the reference, whose distance test is FP64 only
+ * (tracing/refinement.cpp:19-31, geometry/geometry.h:40-48).  With
+ * precision_mode 1 the refine stage decides each pair with an FP32 screen and
+ * re-tests in FP64 only the pairs inside the guard band; this probe measures
+ * that screen on the last step's positions.  It samples the pairs (i, i + o),
+ * o = 1..32, of leaf-major ranks i = 0, stride, 2 stride, ..., and compares the
+ * screen's FP32 distance d32 with the reference's FP64 Point::distance d64
+ * and the screen's decision with the FP64 decision.  Works in either
+ * precision mode; waits for the context's stream; leaves the step's
+ * statistics untouched.  GLINT_ERR_STATE before the first step. */
+typedef struct glint_precision_report {
+    uint64_t pairs;                /* sampled pairs */
+    uint64_t in_band;              /* pairs the screen leaves to the FP64 test */
+    uint64_t mismatches;           /* pairs the screen decides against the FP64 test (0 by construction) */
+    uint64_t contacts;             /* pairs within reach by the FP64 test */
+    double max_abs_err_m;          /* max |d32 - d64| over the sampled pairs, metres */
+    double max_abs_err_near_m;     /* the same over pairs with d64 <= 2 r */
+    double max_band_m;             /* widest guard band met, as a distance either side of r, metres */
+    uint32_t stride;
+    uint32_t reserved;
+} glint_precision_report;
+glint_status glint_precision_probe(glint_ctx *ctx, uint32_t stride, glint_precision_report *out);
+
 /* ---- batching form: many independent regions on one GPU ------------------
  * Each region is a context created from cfgs[r] (its step captured as a CUDA
  * graph, per-stage timing off) with its own stream.  glint_batch_step

@@ -245,3 +245,32 @@ def test_graph_mode_parity():
         rt.cudaFree(buf)
         g.close()
         o.close()
+
+
+def test_precision_probe_screen_agrees_with_fp64():
+    """glint_precision_probe: on every sampled pair the FP32 screen's decision
+    equals the FP64 test's (or defers to it inside the band), the screen's
+    distance error near the reach stays inside the guard band, and the report
+    does not depend on the precision mode the steps ran in."""
+    name = "dense_20k"
+    box, pts = make_points(name, 12)
+    cfgd = case_config(name)
+    n = cfgd["num_objects"]
+    reps = {}
+    for mode in (0, 1):
+        g = DeviceBench(gpu_config(cfgd, precision_mode=mode), box, pts[0])
+        try:
+            for t in range(pts.shape[0]):
+                g.step(pts[t], t)
+            reps[mode] = {s: g.precision_probe(s) for s in (1, 7)}
+        finally:
+            g.close()
+    for s, rep in reps[1].items():
+        expect = sum(min(32, n - 1 - i) for i in range(0, n, s))
+        assert rep["pairs"] == expect, (s, rep)
+        assert rep["mismatches"] == 0, rep
+        assert 0 < rep["contacts"] <= rep["pairs"], rep
+        assert rep["in_band"] <= rep["pairs"], rep
+        assert 0.0 < rep["max_abs_err_near_m"] < rep["max_band_m"] < 1e-4, rep
+        assert rep["max_abs_err_near_m"] <= rep["max_abs_err_m"], rep
+        assert rep == reps[0][s], (rep, reps[0][s])
