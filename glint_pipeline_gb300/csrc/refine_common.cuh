@@ -10,7 +10,8 @@
 
 namespace glint {
 
-constexpr int kQueue = 64;
+constexpr int kQueue = 96;      /* a drain of 64 plus one enqueue of up to 32 */
+constexpr uint32_t kDrainAt = 64;
 constexpr uint32_t kProbeLimit = 1u << 22;
 
 struct QEntry {
@@ -48,13 +49,12 @@ struct RefineArgs {
 /* The table as it stood at the start of the step: keys do not change while
  * the refine kernels run.  Found -> touch the entry (tag, f32 box; each pair
  * has at most one event per step, so the box needs no atomics).  Not found
- * before an empty slot -> the pair is new this step. */
-__device__ inline bool table_touch(const RefineArgs &a, const QEntry &q, uint32_t tag) {
-    uint64_t slot = fastmod(cantor(pair_a(q.pw), pair_b(q.pw)), a.B, a.Bm);
+ * before an empty slot -> the pair is new this step.  The walk starts at the
+ * home slot, whose key word and box the caller has already loaded. */
+__device__ inline bool table_touch_from(const RefineArgs &a, const QEntry &q, uint64_t slot, unsigned long long w0,
+                                        uint4 m, uint32_t tag) {
     for (uint32_t probe = 0; probe < kProbeLimit; ++probe) {
-        const unsigned long long w0 = a.tab[slot].w0;
         if (w0 == q.pw) {
-            uint4 m = *reinterpret_cast<const uint4 *>(a.tab[slot].mbr);
             const uint32_t lx = min(fenc(q.x1), fenc(q.x2)), hx = max(fenc(q.x1), fenc(q.x2));
             const uint32_t ly = min(fenc(q.y1), fenc(q.y2)), hy = max(fenc(q.y1), fenc(q.y2));
             if (lx < m.x || ly < m.y || hx > m.z || hy > m.w) {
@@ -69,38 +69,63 @@ __device__ inline bool table_touch(const RefineArgs &a, const QEntry &q, uint32_
         }
         if (w0 == kEmptyW0) return true;
         slot = (slot + 1 == a.B) ? 0 : slot + 1;
+        w0 = a.tab[slot].w0;
+        m = *reinterpret_cast<const uint4 *>(a.tab[slot].mbr);
     }
     atomicOr(&a.cnt->error_flags, GLINT_EF_TABLE_FULL);
     return false;
 }
 
-/* warp-collective: process queue entries [0, n) one per lane */
+__device__ inline uint64_t home_slot(const RefineArgs &a, unsigned long long pw) {
+    return fastmod(cantor(pair_a(pw), pair_b(pw)), a.B, a.Bm);
+}
+
+/* warp-collective: the lanes whose pair is new append it to the new list */
+__device__ inline void append_new(const RefineArgs &a, bool isnew, const QEntry &q) {
+    const int lane = threadIdx.x & 31;
+    const unsigned m = __ballot_sync(0xffffffffu, isnew);
+    if (!m) return;
+    unsigned long long off = 0;
+    const int leader = __ffs(m) - 1;
+    if (lane == leader) off = atomicAdd(&a.cnt->new_keys, (unsigned long long)__popc(m));
+    off = __shfl_sync(0xffffffffu, off, leader);
+    if (isnew) {
+        const unsigned long long idx = off + __popc(m & ((1u << lane) - 1u));
+        if (idx < a.new_cap) {
+            a.newlist[idx].key = q.pw;
+            a.newlist[idx].prio = q.prio;
+        } else {
+            atomicOr(&a.cnt->error_flags, GLINT_EF_NEW_OVERFLOW);
+        }
+    }
+}
+
+/* warp-collective: process queue entries [0, n), two per lane, with both
+ * home records requested before either is used (the table is far larger
+ * than L2, so each is a DRAM round trip) */
 __device__ inline void drain_queue(const RefineArgs &a, QEntry *Q, uint32_t n, uint32_t tag) {
     const int lane = threadIdx.x & 31;
-    for (uint32_t base = 0; base < n; base += 32) {
-        const uint32_t e = base + lane;
-        bool isnew = false;
-        QEntry q;
-        if (e < n) {
-            q = Q[e];
-            isnew = table_touch(a, q, tag);
+    for (uint32_t base = 0; base < n; base += 64) {
+        const uint32_t e0 = base + lane, e1 = base + 32 + lane;
+        const bool v0 = e0 < n, v1 = e1 < n;
+        QEntry q0, q1;
+        uint64_t s0 = 0, s1 = 0;
+        if (v0) {
+            q0 = Q[e0];
+            s0 = home_slot(a, q0.pw);
         }
-        const unsigned m = __ballot_sync(0xffffffffu, isnew);
-        if (m) {
-            unsigned long long off = 0;
-            const int leader = __ffs(m) - 1;
-            if (lane == leader) off = atomicAdd(&a.cnt->new_keys, (unsigned long long)__popc(m));
-            off = __shfl_sync(0xffffffffu, off, leader);
-            if (isnew) {
-                const unsigned long long idx = off + __popc(m & ((1u << lane) - 1u));
-                if (idx < a.new_cap) {
-                    a.newlist[idx].key = q.pw;
-                    a.newlist[idx].prio = q.prio;
-                } else {
-                    atomicOr(&a.cnt->error_flags, GLINT_EF_NEW_OVERFLOW);
-                }
-            }
+        if (v1) {
+            q1 = Q[e1];
+            s1 = home_slot(a, q1.pw);
         }
+        /* out-of-range lanes read slot 0, which exists, and ignore it */
+        const unsigned long long w00 = a.tab[s0].w0, w01 = a.tab[s1].w0;
+        const uint4 m0 = *reinterpret_cast<const uint4 *>(a.tab[s0].mbr);
+        const uint4 m1 = *reinterpret_cast<const uint4 *>(a.tab[s1].mbr);
+        const bool n0 = v0 && table_touch_from(a, q0, s0, w00, m0, tag);
+        const bool n1 = v1 && table_touch_from(a, q1, s1, w01, m1, tag);
+        append_new(a, n0, q0);
+        append_new(a, n1, q1);
     }
     __syncwarp();
 }
@@ -121,10 +146,10 @@ __device__ inline void enqueue(const RefineArgs &a, QEntry *Q, uint32_t &qn, boo
     }
     qn += __popc(m);
     __syncwarp();
-    if (qn >= 32) {
-        drain_queue(a, Q, 32, tag);
-        const uint32_t rest = qn - 32;
-        if ((uint32_t)lane < rest) Q[lane] = Q[32 + lane];
+    if (qn >= kDrainAt) {
+        drain_queue(a, Q, kDrainAt, tag);
+        const uint32_t rest = qn - kDrainAt;
+        if ((uint32_t)lane < rest) Q[lane] = Q[kDrainAt + lane];
         __syncwarp();
         qn = rest;
     }
