@@ -29,12 +29,15 @@ constexpr uint64_t kKeyMask = (1ULL << 62) - 1;
 
 enum : uint8_t { kInvalid = 0, kBranch = 1, kLeaf = 2 }; /* index/QTree.h:43-47 */
 
-/* stamp byte per table slot: 0 empty, 1 committed entry, 3 entry inserted
- * during the current step (4: reported this step, identify only).  Which step
- * last touched a committed entry is its tag, 1 or 2 by step parity, in the
- * high half of the record's w1 (the low half holds the start time), so a
- * touch writes only the record it has just read. */
-enum : uint8_t { kStampEmpty = 0, kStampOld = 1, kStampNew = 3 };
+/* stamp byte per table slot: 0 empty (or filled during the current step), 1
+ * committed entry (4: reported this step, identify only).  Which step last
+ * touched a committed entry is its tag, 1 or 2 by step parity, in the high
+ * half of the record's w1 (the low half holds the start time), so a touch
+ * writes only the record it has just read.  A slot filled during the step
+ * carries kNewFlag in its key word; the insert marks its 128-byte line (four
+ * slots) in a bitmap small enough to stay in L2 instead of writing a stamp
+ * byte, which would cost a random DRAM read-modify-write per new pair. */
+enum : uint8_t { kStampEmpty = 0, kStampOld = 1 };
 __host__ __device__ inline uint8_t stamp_of(uint64_t step_index) { return (uint8_t)(1 + (step_index & 1)); }
 
 /* ---- exact comparisons without the FP64 pipe --------------------------------

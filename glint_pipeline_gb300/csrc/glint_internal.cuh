@@ -179,6 +179,7 @@ struct glint_ctx {
     /* table */
     glint::TRec *d_tab = nullptr;
     uint8_t *d_stamp = nullptr;
+    uint32_t *d_newline = nullptr;   /* one bit per 4 slots filled this step */
     glint::NewEntry *d_new = nullptr;
     uint32_t *d_tile_cnt = nullptr, *d_tile_off = nullptr;
     uint64_t n_tiles = 0;

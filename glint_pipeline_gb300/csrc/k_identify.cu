@@ -8,9 +8,10 @@
  * min_meet_time + 1.  With one thread the reports come out in bucket order
  * (batch_meet, tracing/meeting.cpp:11-24).
  *
- * Device form: a stamp byte per bucket says empty / touched at this step /
- * touched at the previous step, so the scan reads one byte per bucket and the
- * 32-byte record only of entries that change.  Pass 1 (32 consecutive buckets
+ * Device form: a stamp byte per bucket says empty or committed, and a bit per
+ * 128-byte line of the table says that the insert placed a pair in it this
+ * step, so the scan reads one byte per bucket and the 32-byte records only of
+ * committed entries and of lines that received a pair.  Pass 1 (32 consecutive buckets
  * per warp and round) finalises entries inserted this step, removes expired
  * entries that are too short, marks the ones to report and counts them per
  * 8192-bucket tile; an exclusive scan gives every tile its offset; pass 2
@@ -33,41 +34,52 @@ constexpr uint8_t kStampEmit = 4;
  * the records of kIdIlp rounds are requested before any is used. */
 constexpr int kIdIlp = 4;
 
-__global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict__ stamp, TRec *__restrict__ tab,
-                                                             uint64_t B, uint32_t min_plus1,
+__global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict__ stamp,
+                                                             uint32_t *__restrict__ newline,
+                                                             TRec *__restrict__ tab, uint64_t B, uint32_t min_plus1,
                                                              uint32_t *__restrict__ tile_cnt,
                                                              const float2 *__restrict__ fpos, uint32_t N,
                                                              DevCounters *cnt) {
     __shared__ uint32_t red[3][kIdThreads / 32];
     __shared__ __align__(16) uint8_t sst[kIdThreads / 32][kIdWarpSpan];
+    __shared__ uint32_t snl[kIdThreads / 32][kIdWarpSpan / 128];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint64_t wbase = (uint64_t)blockIdx.x * kIdTile + (uint64_t)wid * kIdWarpSpan;
     const uint32_t cur_time = cnt->step_time, st_now = cnt->step_tag;
-    /* stamps are allocated to a whole number of tiles */
+    /* stamps and new-line words are allocated to a whole number of tiles */
     const uint4 *src = reinterpret_cast<const uint4 *>(stamp + wbase);
     uint4 *dst = reinterpret_cast<uint4 *>(sst[wid]);
     dst[lane] = src[lane];
     dst[lane + 32] = src[lane + 32];
+    if (lane < (int)(kIdWarpSpan / 128)) {
+        /* the warp's lines filled this step; cleared for the next step */
+        snl[wid][lane] = newline[(wbase >> 7) + lane];
+        newline[(wbase >> 7) + lane] = 0;
+    }
     __syncwarp();
     uint32_t emit = 0, taken = 0, active = 0;
     for (uint32_t r0 = 0; r0 < kIdWarpSpan / 32; r0 += kIdIlp) {
         uint8_t sv[kIdIlp];
+        bool need[kIdIlp];
         ulonglong2 rec[kIdIlp];
 #pragma unroll
         for (int u = 0; u < kIdIlp; ++u) {
             const uint32_t off = (r0 + u) * 32 + lane;
             sv[u] = wbase + off < B ? sst[wid][off] : kStampEmpty;
-            if (sv[u] != kStampEmpty) rec[u] = *reinterpret_cast<const ulonglong2 *>(&tab[wbase + off]);
+            need[u] = sv[u] != kStampEmpty || (wbase + off < B && ((snl[wid][off >> 7] >> ((off >> 2) & 31)) & 1u));
+            if (need[u]) rec[u] = *reinterpret_cast<const ulonglong2 *>(&tab[wbase + off]);
         }
 #pragma unroll
         for (int u = 0; u < kIdIlp; ++u) {
-            if (sv[u] == kStampEmpty) continue;
+            if (!need[u]) continue;
             const uint64_t b = wbase + (r0 + u) * 32 + lane;
-            ++taken;
             TRec &r = tab[b];
-            if (sv[u] == kStampNew) {
-                /* a pair inserted this step: start = now and the f32 box of
-                 * its two points (geometry.cu:481-489) */
+            if (sv[u] == kStampEmpty) {
+                /* a slot of a line that received a pair this step: empty, or
+                 * the pair (key word with kNewFlag).  Its start is now and its
+                 * box that of its two points (geometry.cu:481-489). */
+                if (rec[u].x == kEmptyW0 || !(rec[u].x & kNewFlag)) continue;
+                ++taken;
                 ++active;
                 const unsigned long long pw = rec[u].x & kPairMask;
                 const uint32_t pa = pair_a(pw), pb = pair_b(pw);
@@ -88,6 +100,7 @@ __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict
                 stamp[b] = kStampOld;
                 continue;
             }
+            ++taken;
             const unsigned long long w1 = rec[u].y;
             if ((uint32_t)(w1 >> 32) == st_now) {
                 ++active;
@@ -193,7 +206,8 @@ cudaError_t launch_identify(glint_ctx *c, uint32_t cur_time) {
     cudaStream_t s = c->stream;
     const uint64_t tiles = identify_tiles(c->B);
     const uint32_t min_plus1 = c->cfg.min_meet_time + 1;
-    k_expire_count<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, min_plus1, c->d_tile_cnt,
+    k_expire_count<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_newline, c->d_tab, c->B, min_plus1,
+                                                          c->d_tile_cnt,
                                                           c->d_fpos, c->N, c->d_cnt);
     scan_u32(c->d_tile_cnt, c->d_tile_off, tiles, c->d_scan_tmp, s);
     k_expire_emit<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_tab, c->B, c->d_tile_cnt, c->d_tile_off,

@@ -214,7 +214,7 @@ __device__ inline void touch_box(TRec &r, const float2 &A, const float2 &Bp) {
     *reinterpret_cast<uint4 *>(r.mbr) = m;
 }
 
-__global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ list, TRec *tab, uint8_t *stamp,
+__global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ list, TRec *tab, uint32_t *newline,
                                                 uint64_t B, uint64_t Bm, uint64_t new_cap,
                                                 const float2 *__restrict__ fpos, uint32_t N,
                                                 DevCounters *cnt) {
@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ lis
                 if (seen.x == kEmptyW0) {
                     ulonglong2 prev = cas128(&tab[slot], seen, cur);
                     if (u128_eq(prev, seen)) {
-                        stamp[slot] = kStampNew;
+                        atomicOr(&newline[slot >> 7], 1u << ((slot >> 2) & 31));
                         done = true;
                         break;
                     }
@@ -280,7 +280,7 @@ __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ lis
 
 cudaError_t launch_insert(glint_ctx *c, uint32_t cur_time) {
     (void)cur_time;
-    k_insert<<<152 * 8, 256, 0, c->stream>>>(c->d_new, c->d_tab, c->d_stamp, c->B, c->Bm, c->new_cap, c->d_fpos, c->N,
+    k_insert<<<152 * 8, 256, 0, c->stream>>>(c->d_new, c->d_tab, c->d_newline, c->B, c->Bm, c->new_cap, c->d_fpos, c->N,
                                              c->d_cnt);
     return cudaGetLastError();
 }
