@@ -191,8 +191,8 @@ def stage_bytes(stage, N, st, K):
         return 24 * N + 36 * st["border_objects"] + 24 * st["cross_checks"]
     if stage == "insert":
         # per new pair: list entry (16 B), record compare-and-swap read and
-        # write (64 B), stamp (1 B)
-        return 81 * st["new_keys"]
+        # write (64 B); the line bitmap it marks stays in L2
+        return 80 * st["new_keys"]
     if stage == "partition":
         # point and order reads, three leaf words, scatter, segment sort, and
         # the gather of six per-object arrays
@@ -282,23 +282,33 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
     rt.cudaFree(tmp)
     arr = (ctypes.c_double * (2 * N * ke)).from_address(hbuf.value)
     host = np.frombuffer(arr, dtype=np.float64).reshape(ke, N, 2)
+    # the step's meetings come back into page-locked memory, as its points
+    # go in from it
+    mbuf = gp.pinned_empty(N, _abi.MEETING_DTYPE)
     barrier(pg)
     d2h = 0
     t0 = time.perf_counter()
     for k in range(ke):
         bench.step(host[k], base + k)
-        m = bench.meetings()
+        m = bench.meetings(out=mbuf)
         d2h += m.nbytes + ctypes.sizeof(_abi.GlintStepStats)
     dt = allreduce_max(pg, time.perf_counter() - t0)
     out["e2e"] = {"value": N * ke * world / dt, "unit": UNIT, "h2d_bytes_per_step": step_bytes,
                   "d2h_bytes_per_step": int(d2h / ke), "steps": ke}
-    del host, arr
+    del host, arr, m, mbuf
     rt.cudaFreeHost(hbuf)
     out["_bench"] = bench
     return out
 
 
-def roofline(form, N):
+# DRAM bytes per step of each stage's kernels (dram__bytes_read.sum +
+# dram__bytes_write.sum) from the one-pass ncu launch list of the tuned step
+# at 10M objects and 2^30 buckets (profiles/step10m_tuned_dram.md); other
+# workloads report null
+TRAFFIC_10M_2P30 = {"refine": 42.7e9, "identify": 50.3e9, "insert": 26.1e9}
+
+
+def roofline(form, N, buckets=None, mode=None):
     pk = peaks()
     hbm = pk.get("hbm_gbs")
     stages = {k: v for k, v in form["stage_ms"].items() if k in ("partition", "filter", "refine", "insert", "identify")}
@@ -307,8 +317,12 @@ def roofline(form, N):
     by = stage_bytes(top, N, form["per_step"], 1)
     achieved = by / (ms / 1000.0) / 1e9 if ms > 0 else None
     peak = hbm if hbm else 6800.0
+    traffic = None
+    if N == 10_000_000 and buckets == 1 << 30 and mode == "tuned" and top in TRAFFIC_10M_2P30:
+        traffic = TRAFFIC_10M_2P30[top]
     return {"kernel_stage": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak if achieved else None, "traffic": None, "algorithmic_bytes": by,
+            "frac": achieved / peak if achieved else None, "traffic": traffic,
+            "traffic_unit": "bytes per step of the stage's kernels (ncu launch list)", "algorithmic_bytes": by,
             "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "of fallback"}
 
 
@@ -751,7 +765,7 @@ def main():
                                        f"buckets, flush past 2^26 keys; headline form '{modes[0]}'",
                            "objects": N, "buckets": args.buckets, "form": modes[0],
                            "l2": "inputs larger than L2 (160 MB of points per step, 34 GB table)"},
-                "roofline": roofline(head, N), "clocks": head["clocks"], "e2e": head["e2e"], "cpu_baseline": cpu,
+                "roofline": roofline(head, N, args.buckets, modes[0]), "clocks": head["clocks"], "e2e": head["e2e"], "cpu_baseline": cpu,
                 "gpu_launches": head["gpu_launches"], "serving": serve,
                 "forms": {m: {k: v for k, v in f.items()} for m, f in forms.items()}}
         print(json.dumps(line), flush=True)

@@ -133,12 +133,21 @@ class DeviceBench:
             raise GlintError(st, self.last_error())
         return stats
 
-    def meetings(self) -> np.ndarray:
-        """Meetings identified by the last step, in bucket order."""
+    def meetings(self, out: np.ndarray | None = None) -> np.ndarray:
+        """Meetings identified by the last step, in bucket order.  With `out`
+        (MEETING_DTYPE records, e.g. from pinned_empty) large enough, they
+        are copied into it and out[:n] is returned; otherwise into a new
+        array."""
         n = ctypes.c_uint64()
         st = self.lib.glint_meetings(self.h, None, 0, ctypes.byref(n))
         if st != 0:
             raise GlintError(st, self.last_error())
+        if out is not None and out.dtype == MEETING_DTYPE and out.flags.c_contiguous and out.shape[0] >= n.value:
+            if n.value:
+                st = self.lib.glint_meetings(self.h, out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n))
+                if st != 0:
+                    raise GlintError(st, self.last_error())
+            return out[: n.value]
         out = np.zeros(n.value, dtype=MEETING_DTYPE)
         if n.value:
             st = self.lib.glint_meetings(self.h, out.ctypes.data_as(ctypes.c_void_p), n.value, ctypes.byref(n))
@@ -360,6 +369,24 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def pinned_empty(shape, dtype) -> np.ndarray:
+    """An uninitialised array in page-locked host memory (glint_host_alloc),
+    released when the array and its views are gone."""
+    import weakref
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape))
+    nbytes = max(count * dt.itemsize, 1)
+    lib = _abi.lib()
+    p = ctypes.c_void_p()
+    st = lib.glint_host_alloc(nbytes, ctypes.byref(p))
+    if st != 0 or not p.value:
+        raise GlintError(st, "glint_host_alloc")
+    raw = (ctypes.c_uint8 * nbytes).from_address(p.value)
+    arr = np.frombuffer(raw, dtype=np.uint8, count=count * dt.itemsize).view(dt).reshape(shape)
+    weakref.finalize(raw, lib.glint_host_free, ctypes.c_void_p(p.value))
+    return arr
 
 
 def cuda_create_device_bench(config: Configuration, mbr, first_points=None, schema=None) -> DeviceBench:

@@ -207,6 +207,8 @@ def load_library(path: str | None = None):
     lib.glint_server_poll.argtypes = [vp, u64, ctypes.POINTER(GlintQueryResult), ctypes.POINTER(ctypes.c_int)]
     lib.glint_store_read.argtypes = [vp] * 9 + [ctypes.POINTER(GlintStoreInfo)]
     lib.glint_active_search_noalloc.argtypes = [vp, vp, u32, vp, u64, vp]
+    lib.glint_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(vp)]
+    lib.glint_host_free.argtypes = [vp]
     lib.glint_precision_probe.argtypes = [vp, u32, ctypes.POINTER(GlintPrecisionReport)]
     lib.glint_batch_create.argtypes = [u32, vp, vp, vp, ctypes.POINTER(vp)]
     lib.glint_batch_destroy.argtypes = [vp]

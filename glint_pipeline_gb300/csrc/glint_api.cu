@@ -717,6 +717,22 @@ glint_status glint_step(glint_ctx *c, const double *points, uint32_t cur_time, g
     return glint_sync(c, st);
 }
 
+glint_status glint_host_alloc(size_t bytes, void **out) {
+    if (!out) return GLINT_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    const cudaError_t e = cudaMallocHost(out, bytes ? bytes : 1);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return e == cudaErrorMemoryAllocation ? GLINT_ERR_OUT_OF_MEMORY : GLINT_ERR_CUDA;
+    }
+    return GLINT_OK;
+}
+
+glint_status glint_host_free(void *p) {
+    if (p && cudaFreeHost(p) != cudaSuccess) return GLINT_ERR_CUDA;
+    return GLINT_OK;
+}
+
 glint_status glint_meetings(glint_ctx *c, glint_meeting *out, uint64_t cap, uint64_t *n) {
     if (!c) return GLINT_ERR_INVALID_ARGUMENT;
     cudaError_t e = cudaStreamSynchronize(c->stream);

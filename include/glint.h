@@ -216,6 +216,15 @@ glint_status glint_get_capacities(const glint_ctx *ctx, uint32_t *schema_capacit
 /* the context's cudaStream_t */
 void *glint_stream(glint_ctx *ctx);
 
+/* Page-locked host memory (cudaMallocHost) for step inputs and results:
+ * glint_step's copy of the points and glint_meetings' copy of the meetings
+ * run at the full host link rate from and into it, where pageable memory is
+ * staged by the driver.  No counterpart in the reference, which reads traces
+ * into pageable buffers (tracing/process.cpp:128-144).  *out is NULL on
+ * failure. */
+glint_status glint_host_alloc(size_t bytes, void **out);
+glint_status glint_host_free(void *p);
+
 /* ---- flush into the sorted key-value + bitmap store ------------------------
  * Every identified meeting whose box lies inside the map becomes two keys
  * (cuda/geometry.cu:665-734): [sid:12][pid:26][target:26][duration:32]

@@ -274,3 +274,28 @@ def test_precision_probe_screen_agrees_with_fp64():
         assert 0.0 < rep["max_abs_err_near_m"] < rep["max_band_m"] < 1e-4, rep
         assert rep["max_abs_err_near_m"] <= rep["max_abs_err_m"], rep
         assert rep == reps[0][s], (rep, reps[0][s])
+
+
+def test_meetings_into_pinned_buffer():
+    """glint_meetings into page-locked memory from glint_host_alloc gives the
+    same records as into a fresh array, step after step (the buffer is
+    reused)."""
+    from glint_pipeline_gb300 import pinned_empty
+    from glint_pipeline_gb300._abi import MEETING_DTYPE
+    name = "dense_20k"
+    box, pts = make_points(name, 20)
+    cfgd = case_config(name)
+    g = DeviceBench(gpu_config(cfgd, precision_mode=1), box, pts[0])
+    buf = pinned_empty(cfgd["num_objects"], MEETING_DTYPE)
+    seen = 0
+    try:
+        for t in range(pts.shape[0]):
+            g.step(pts[t], t)
+            a = g.meetings()
+            b = g.meetings(out=buf)
+            assert b.base is not None and b.shape == a.shape
+            np.testing.assert_array_equal(a.view(np.uint8), b.view(np.uint8))
+            seen += a.shape[0]
+        assert seen > 0
+    finally:
+        g.close()
