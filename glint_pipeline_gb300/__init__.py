@@ -216,6 +216,20 @@ class DeviceBench:
         out["info"] = info
         return out
 
+    def dump_store(self, raid_path: str, meta_path: str, prefix: str, ctb: int = 0):
+        """The last flush's store into files in the reference's layout
+        (straight_dump, tracing/process.cpp:254-348)."""
+        st = self.lib.glint_store_dump(self.h, raid_path.encode(), meta_path.encode(), prefix.encode(), int(ctb))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+
+    def load_store(self, raid_path: str, meta_path: str, prefix: str, ctb: int = 0):
+        """One block's files (written here or by the reference) into a kept
+        block for queries (workbench::load_CTB_meta and friends)."""
+        st = self.lib.glint_store_load(self.h, raid_path.encode(), meta_path.encode(), prefix.encode(), int(ctb))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+
     def store_blocks(self) -> int:
         return int(self.lib.glint_store_blocks(self.h))
 
@@ -369,6 +383,27 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+def write_store_files(store: dict, info, num_objects: int, raid_path: str, meta_path: str, prefix: str,
+                      ctb: int = 0):
+    """Host store arrays (as DeviceBench.store() returns them; `info` a
+    glint_store_info-layout structure) into files in the reference's layout,
+    without a device (glint_store_write)."""
+    lib = _abi.lib()
+    C = int(store["ctfs"].shape[0])
+    arrs = {k: np.ascontiguousarray(store[k]) for k in ("keys", "sids", "ctfs", "bitmaps", "o_keys", "o_boxes",
+                                                        "o_bitmap")}
+    v = _abi.GlintStoreView()
+    v.num_objects, v.CTF_count = int(num_objects), C
+    ptr = lambda a: a.ctypes.data if a.size else None  # noqa: E731
+    v.keys, v.sids, v.ctfs, v.bitmaps = ptr(arrs["keys"]), ptr(arrs["sids"]), ptr(arrs["ctfs"]), ptr(arrs["bitmaps"])
+    v.oversize_keys, v.oversize_boxes, v.oversize_bitmap = ptr(arrs["o_keys"]), ptr(arrs["o_boxes"]), \
+        ptr(arrs["o_bitmap"])
+    ctypes.memmove(ctypes.addressof(v.info), ctypes.addressof(info), ctypes.sizeof(v.info))
+    st = lib.glint_store_write(ctypes.byref(v), raid_path.encode(), meta_path.encode(), prefix.encode(), int(ctb))
+    if st != 0:
+        raise GlintError(st, lib.glint_store_file_error().decode())
 
 
 def pinned_empty(shape, dtype) -> np.ndarray:

@@ -141,6 +141,13 @@ class GlintStoreInfo(ctypes.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
 
 
+class GlintStoreView(ctypes.Structure):
+    _fields_ = [("num_objects", ctypes.c_uint32), ("CTF_count", ctypes.c_uint32), ("keys", ctypes.c_void_p),
+                ("sids", ctypes.c_void_p), ("ctfs", ctypes.c_void_p), ("bitmaps", ctypes.c_void_p),
+                ("oversize_keys", ctypes.c_void_p), ("oversize_boxes", ctypes.c_void_p),
+                ("oversize_bitmap", ctypes.c_void_p), ("info", GlintStoreInfo)]
+
+
 class GlintQuery(ctypes.Structure):
     _fields_ = [("seeds", ctypes.c_void_p), ("n_seeds", ctypes.c_uint32), ("hops", ctypes.c_uint32),
                 ("t_start", ctypes.c_uint32), ("t_end", ctypes.c_uint32)]
@@ -207,6 +214,11 @@ def load_library(path: str | None = None):
     lib.glint_server_poll.argtypes = [vp, u64, ctypes.POINTER(GlintQueryResult), ctypes.POINTER(ctypes.c_int)]
     lib.glint_store_read.argtypes = [vp] * 9 + [ctypes.POINTER(GlintStoreInfo)]
     lib.glint_active_search_noalloc.argtypes = [vp, vp, u32, vp, u64, vp]
+    lib.glint_store_write.argtypes = [ctypes.POINTER(GlintStoreView), ctypes.c_char_p, ctypes.c_char_p,
+                                      ctypes.c_char_p, u32]
+    lib.glint_store_file_error.restype = ctypes.c_char_p
+    lib.glint_store_dump.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
+    lib.glint_store_load.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
     lib.glint_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(vp)]
     lib.glint_host_free.argtypes = [vp]
     lib.glint_precision_probe.argtypes = [vp, u32, ctypes.POINTER(GlintPrecisionReport)]

@@ -276,6 +276,45 @@ glint_status glint_store_read(glint_ctx *ctx, uint8_t *keys, uint16_t *sids, uin
                               glint_ctf_meta *ctfs, uint8_t *bitmaps, void *oversize_keys, float *oversize_boxes,
                               uint8_t *oversize_bitmap, glint_store_info *info);
 
+/* ---- the store on disk, in the reference's file layout ----------------------
+ * straight_dump (tracing/process.cpp:254-348) writes a flushed block `ctb` as
+ *   <raid_path><i % 2>/<prefix>_SSTable_<ctb>-<i>  CTF i's packed keys
+ *   <meta_path>/<prefix>_CTB<ctb>                  CTB record, sids, oversize
+ *                                                  keys, boxes and bitmap
+ *   <meta_path>/<prefix>_STcL<ctb>-<i>             CTF record + its bitmap
+ * (workbench::dump_CTB_meta, CTF::dump_meta: tracing/workbench.cpp:597-614,
+ * tracing/step_merge.cpp:644-650), and workbench::load_CTB_meta /
+ * load_CTF_meta / load_CTF_keys (tracing/workbench.cpp:302-325, 639-695) read
+ * it back; the reference's prefix is "6oversize_<file_size>".  The records
+ * have the reference's LP64 layouts (CTF 80 bytes, CTB 128); their pointer
+ * fields are written as zero.  Directories must exist. */
+typedef struct glint_store_view {
+    uint32_t num_objects, CTF_count;
+    const uint8_t *keys;               /* packed CTF keys, info.key_bytes */
+    const uint16_t *sids;              /* num_objects */
+    const glint_ctf_meta *ctfs;        /* CTF_count */
+    const uint8_t *bitmaps;            /* CTF_count * 8192 bytes */
+    const void *oversize_keys;         /* 16-byte little-endian keys */
+    const float *oversize_boxes;       /* 4 floats per key */
+    const uint8_t *oversize_bitmap;    /* 8192 bytes */
+    glint_store_info info;
+} glint_store_view;
+/* host arrays (as glint_store_read fills them) into files; no device work */
+glint_status glint_store_write(const glint_store_view *store, const char *raid_path, const char *meta_path,
+                               const char *prefix, uint32_t ctb);
+/* the failure message of the last glint_store_write on this thread */
+const char *glint_store_file_error(void);
+/* the last flush's store into files */
+glint_status glint_store_dump(glint_ctx *ctx, const char *raid_path, const char *meta_path, const char *prefix,
+                              uint32_t ctb);
+/* files of one block, written here or by the reference, into a block kept
+ * on the device for glint_query_batch and servers (the oldest kept block is
+ * dropped beyond glint_config.store_keep; GLINT_ERR_STATE when it is 0).  The
+ * key end offsets are rebased on the CTF records' end_time_min, the window
+ * base the flush wrote there. */
+glint_status glint_store_load(glint_ctx *ctx, const char *raid_path, const char *meta_path, const char *prefix,
+                              uint32_t ctb);
+
 /* ---- contact-trace queries over the flushed store ---------------------------
  * The reference reads its store per object (id_search_in_CTB,
  * tracing/workbench.cpp:397-444): the object's sid picks its CTF or the

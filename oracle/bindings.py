@@ -363,6 +363,13 @@ def ref_lib():
                                        ctypes.c_uint64, vp]
         lib.ref_ctf_find.restype = ctypes.c_int
         lib.ref_ctf_find.argtypes = [vp, vp, vp, ctypes.c_uint32, ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32)]
+        lib.ref_store_load.restype = vp
+        lib.ref_store_load.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32,
+                                       ctypes.c_uint32, ctypes.c_uint32]
+        lib.ref_store_get.argtypes = [vp] * 9
+        lib.ref_store_find.restype = ctypes.c_uint32
+        lib.ref_store_find.argtypes = [vp, ctypes.c_uint32]
+        lib.ref_store_free.argtypes = [vp]
         _REF = lib
     return _REF
 

@@ -277,4 +277,111 @@ int ref_ctf_find(const float *ctf_mbr4, const uint16_t *bits, const uint8_t *key
     return find;
 }
 
+/* ---- the reference's readers of a dumped block (workbench::load_CTB_meta,
+ * load_CTF_meta, load_CTF_keys, tracing/workbench.cpp:302-325, 639-695), used
+ * to pin the file layout of glint_store_write ---- */
+struct ref_store {
+    configuration *config;
+    workbench *bench;
+    uint32_t ctb;
+};
+
+/* meta_prefix = <meta_path>/<prefix>; raid_path and keys_prefix go into the
+ * reference's fixed-size fields (at most 23 characters) */
+void *ref_store_load(const char *meta_prefix, const char *raid_path, const char *keys_prefix, uint32_t ctb,
+                     uint32_t num_objects, uint32_t CTF_count) {
+    ref_store *h = new ref_store();
+    configuration *c = new configuration();
+    c->num_objects = num_objects;
+    c->CTF_count = CTF_count;
+    std::strncpy(c->raid_path, raid_path, sizeof(c->raid_path) - 1);
+    workbench *b = new workbench(c);
+    b->bit_count = 256 * 256;
+    std::strncpy(b->keys_file_prefix, keys_prefix, sizeof(b->keys_file_prefix) - 1);
+    b->ctbs = new CTB[ctb + 1];
+    b->load_CTB_meta(meta_prefix, (int)ctb);
+    for (uint32_t j = 0; j < CTF_count; ++j) b->load_CTF_keys(ctb, j);
+    h->config = c;
+    h->bench = b;
+    h->ctb = ctb;
+    return h;
+}
+
+/* what the reference read: sids, the oversize buffer (count, times, keys,
+ * boxes, bitmap), every CTF's fields in the 64-byte metadata layout of the
+ * store, its bitmap bytes (ctf_bitmap_size each, slots of 8192) and keys */
+void ref_store_get(void *hv, uint16_t *sids, uint32_t *o_count_times, uint8_t *o_keys, float *o_boxes,
+                   uint8_t *o_bitmap, uint8_t *ctf_meta64, uint8_t *bitmaps, uint8_t *keys) {
+    ref_store *h = (ref_store *)hv;
+    CTB &t = h->bench->ctbs[h->ctb];
+    const uint32_t N = h->config->num_objects, C = h->config->CTF_count;
+    std::memcpy(sids, t.sids, sizeof(uint16_t) * N);
+    const oversize_buffer &o = t.o_buffer;
+    o_count_times[0] = o.oversize_kv_count;
+    o_count_times[1] = o.start_time_min;
+    o_count_times[2] = o.start_time_max;
+    o_count_times[3] = o.end_time_min;
+    o_count_times[4] = o.end_time_max;
+    std::memcpy(o_keys, o.keys, 16 * (size_t)o.oversize_kv_count);
+    std::memcpy(o_boxes, o.boxes, sizeof(f_box) * (size_t)o.oversize_kv_count);
+    std::memcpy(o_bitmap, o.o_bitmaps, 256 * 256 / 8);
+    size_t at = 0;
+    for (uint32_t j = 0; j < C; ++j) {
+        const CTF &f = t.ctfs[j];
+        uint8_t *m = ctf_meta64 + 64 * (size_t)j;
+        std::memset(m, 0, 64);
+        std::memcpy(m, &f.ctf_mbr, 16);
+        const uint32_t u[6] = {f.CTF_kv_capacity, f.start_time_min, f.start_time_max, f.end_time_min, f.end_time_max,
+                               f.ctf_bitmap_size};
+        std::memcpy(m + 16, u, sizeof(u));
+        const uint16_t b[10] = {f.key_bit, f.id_bit, f.duration_bit, f.end_bit, f.low_x_bit,
+                                f.low_y_bit, f.edge_bit, f.mbr_bit,  f.x_grid,  f.y_grid};
+        std::memcpy(m + 40, b, sizeof(b));
+        std::memcpy(bitmaps + (size_t)j * (256 * 256 / 8), f.bitmap, f.ctf_bitmap_size);
+        const size_t n = (size_t)f.key_bit / 8 * f.CTF_kv_capacity;
+        std::memcpy(keys + at, f.keys, n);
+        at += n;
+    }
+}
+
+/* the reference's lookup of one object in the loaded block, as
+ * id_search_in_CTB routes it (tracing/workbench.cpp:397-429): sid 0 -> none,
+ * sid 1 -> oversize_buffer::search_buffer, else CTF::binary_search and the
+ * walk over the object's keys; returns the number of keys of oid */
+uint32_t ref_store_find(void *hv, uint32_t oid) {
+    ref_store *h = (ref_store *)hv;
+    CTB &t = h->bench->ctbs[h->ctb];
+    const uint16_t sid = t.sids[oid];
+    if (sid == 0) return 0;
+    if (sid == 1) {
+        time_query tq;
+        atomic<long long> cnt(0);
+        return t.o_buffer.search_buffer(oid, &tq, false, cnt, nullptr);
+    }
+    CTF &f = t.ctfs[sid - 2];
+    const int find = f.binary_search(oid);
+    if (find < 0) return 0;
+    uint32_t k = 0;
+    const uint8_t *data = reinterpret_cast<const uint8_t *>(f.keys);
+    for (uint32_t i = (uint32_t)find; i < f.CTF_kv_capacity; ++i) {
+        __uint128_t v = 0;
+        std::memcpy(&v, data + (size_t)i * f.key_bit / 8, f.key_bit / 8);
+        if (f.ctf_get_key_oid(v) != oid) break;
+        ++k;
+    }
+    return k;
+}
+
+void ref_store_free(void *hv) {
+    ref_store *h = (ref_store *)hv;
+    if (!h) return;
+    /* the loaded arrays belong to the CTB and CTF objects (new[]); the rest
+     * of the workbench was never allocated */
+    delete[] h->bench->ctbs;
+    h->bench->ctbs = nullptr;
+    delete h->bench;
+    delete h->config;
+    delete h;
+}
+
 } /* extern "C" */

@@ -127,3 +127,42 @@ def test_serving_mix_equals_alone():
             np.testing.assert_array_equal(results[i][h], want[h], err_msg=f"query {i} hop {h + 1} (vs oracle)")
     srv.close()
     g.close()
+
+
+def test_store_files_round_trip(tmp_path, monkeypatch):
+    """glint_store_dump writes the last flushed block in the reference's file
+    layout, byte for byte what glint_store_write makes of the same block read
+    to the host; glint_store_load of those files into a fresh context answers
+    queries as the oracle does over that window's meetings."""
+    import os
+    from glint_pipeline_gb300 import write_store_files
+    monkeypatch.chdir(tmp_path)
+    for d in ("r0", "r1", "m", "h0", "h1", "hm"):
+        os.makedirs(d)
+    g, n, windows = build_store("dense_20k", 40, (20, 39), keep=1)
+    g.dump_store("r", "m", "6oversize_3600", 1)
+    store = g.store()
+    write_store_files(store, store["info"], n, "h", "hm", "6oversize_3600", 1)
+    names = sorted(os.listdir("m"))
+    assert len(names) == 1 + store["ctfs"].shape[0]
+    for name in names:
+        assert open(f"m/{name}", "rb").read() == open(f"hm/{name}", "rb").read(), name
+    for i in range(store["ctfs"].shape[0]):
+        a = open(f"r{i % 2}/6oversize_3600_SSTable_1-{i}", "rb").read()
+        assert a == open(f"h{i % 2}/6oversize_3600_SSTable_1-{i}", "rb").read()
+    box = g.map_box
+    cfg = g.config
+    g.close()
+    f = DeviceBench(cfg, box, make_points("dense_20k", 1)[1][0])
+    try:
+        f.load_store("r", "m", "6oversize_3600", 1)
+        assert f.store_blocks() == 1
+        edges = edges_of(windows[-1], box)
+        rng = np.random.default_rng(9)
+        queries = [(rng.choice(n, k, replace=False).astype(np.uint32), hops, t0, t1)
+                   for k, hops, t0, t1 in [(1, 3, 0, 0), (100, 2, 0, 0), (1000, 3, 0, 0), (50, 2, 24, 34)]]
+        check(f, n, edges, queries)
+        with pytest.raises(Exception):
+            f.load_store("r", "m", "6oversize_3600", 7)   # no such block
+    finally:
+        f.close()
