@@ -128,7 +128,7 @@ __global__ void __launch_bounds__(256) k_keys_append(const glint_meeting *__rest
             a.keys[idx + k] = ((u128)pid << kPidShift) + ((u128)target << 64) + ((u128)duration << 32) +
                               (u128)(uint32_t)(m.end - end_time_min);
             a.boxes[idx + k] = box;
-            if (atomicAdd(&a.same[pid], 1u) == 0) atomicAdd(&cnt->sid_count, 1u);
+            atomicAdd(&a.same[pid], 1u); /* objects with keys are counted at the flush */
             uint32_t *o = reinterpret_cast<uint32_t *>(&a.obox[pid]);
             atomicMin(&o[0], l0);
             atomicMin(&o[1], l1);
@@ -150,10 +150,12 @@ __global__ void __launch_bounds__(256) k_set_oid(uint32_t N, const uint32_t *__r
                                                  double dprob, uint32_t *__restrict__ oids,
                                                  unsigned long long *__restrict__ mid, uint8_t *__restrict__ over,
                                                  DevCounters *cnt) {
+    uint32_t with_keys = 0;
     for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < N; id += gridDim.x * blockDim.x) {
         oids[id] = id;
         unsigned long long m = 0;
         if (same[id] >= 1) {
+            ++with_keys;
             const uint4 o = obox[id];
             const float low0 = u2f_coord(o.x), high0 = u2f_coord(o.z), low1 = u2f_coord(o.y), high1 = u2f_coord(o.w);
             const float area = __fmul_rn(__fsub_rn(high1, low1), __fsub_rn(high0, low0));
@@ -169,6 +171,9 @@ __global__ void __launch_bounds__(256) k_set_oid(uint32_t N, const uint32_t *__r
         mid[id] = m;
         over[id] = 0; /* finalised by k_mark_over once every area cut is in */
     }
+    /* sid_count: objects with at least one key in this window */
+    with_keys = __reduce_add_sync(0xffffffffu, with_keys);
+    if ((threadIdx.x & 31) == 0 && with_keys) atomicAdd(&cnt->sid_count, with_keys);
 }
 
 __global__ void k_mark_over(uint32_t N, const uint16_t *__restrict__ sids, uint8_t *__restrict__ over) {

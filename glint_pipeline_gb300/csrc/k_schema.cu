@@ -214,6 +214,7 @@ __global__ void __launch_bounds__(kStackThreads) k_sch_stacks(uint32_t *__restri
                                                               DevCounters *cnt) {
     extern __shared__ uint32_t sm[];
     __shared__ uint4 chunk[2 * kChunk];
+    __shared__ int32_t lv[kChunk];
     __shared__ int32_t s_min, s_max, s_carry;
     __shared__ uint32_t s_ws[32];
     const uint32_t E = cnt->n_events;
@@ -281,11 +282,13 @@ __global__ void __launch_bounds__(kStackThreads) k_sch_stacks(uint32_t *__restri
         for (uint32_t i = cb + threadIdx.x; i < ce; i += blockDim.x) {
             chunk[2 * (i - cb)] = evdata[2 * i];
             chunk[2 * (i - cb) + 1] = evdata[2 * i + 1];
+            lv[i - cb] = levels[i];
         }
         __syncthreads();
+        /* the serial part touches shared memory only */
         if (threadIdx.x == 0) {
             for (uint32_t i = cb; i < ce; ++i) {
-                const int32_t k = levels[i];
+                const int32_t k = lv[i - cb];
                 const int64_t sp = ssi0 + 4 * (int64_t)k - s_lo;  /* schema_stack_index in the window */
                 const int64_t gp = gsi0 + 3 * (int64_t)k - g_lo;  /* grids_stack_index in the window */
                 uint4 &a = chunk[2 * (i - cb)];
