@@ -17,9 +17,10 @@ store (p50/p99 latency, queries/s).
 
 value: device-resident inputs (every step's points generated on the device
 beforehand), the K timed steps measured with CUDA events on the step's
-stream.  e2e: further steps through glint_step() with points in pinned host
-memory (host->device copy inside the timed region) and each step's meetings
-copied back.  Under torchrun (N>1) every rank runs an independent replica on
+stream.  e2e: further steps through the pipelined API (glint_pipe_*) with
+points in pinned host memory (host->device copy inside the timed region,
+overlapped with the step before) and each step's meetings read back from
+page-locked result buffers.  Under torchrun (N>1) every rank runs an independent replica on
 its own GPU (the path has no data exchange): the slowest rank's time counts
 and value sums all ranks' object-timesteps.
 """
@@ -282,20 +283,25 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
     rt.cudaFree(tmp)
     arr = (ctypes.c_double * (2 * N * ke)).from_address(hbuf.value)
     host = np.frombuffer(arr, dtype=np.float64).reshape(ke, N, 2)
-    # the step's meetings come back into page-locked memory, as its points
-    # go in from it
-    mbuf = gp.pinned_empty(N, _abi.MEETING_DTYPE)
+    # pipelined stepping (glint_pipe_*): step k+1's points are copied from
+    # page-locked memory while step k computes, and each step's meetings are
+    # written into page-locked result buffers and read here
+    pipe = gp.Pipe(bench, result_capacity=N)
     barrier(pg)
     d2h = 0
     t0 = time.perf_counter()
+    pipe.submit(host[0], base)
     for k in range(ke):
-        bench.step(host[k], base + k)
-        m = bench.meetings(out=mbuf)
+        if k + 1 < ke:
+            pipe.submit(host[k + 1], base + k + 1)
+        st_k, m = pipe.result(base + k)
         d2h += m.nbytes + ctypes.sizeof(_abi.GlintStepStats)
     dt = allreduce_max(pg, time.perf_counter() - t0)
+    del m
+    pipe.close()
     out["e2e"] = {"value": N * ke * world / dt, "unit": UNIT, "h2d_bytes_per_step": step_bytes,
                   "d2h_bytes_per_step": int(d2h / ke), "steps": ke}
-    del host, arr, m, mbuf
+    del host, arr
     rt.cudaFreeHost(hbuf)
     out["_bench"] = bench
     return out

@@ -324,6 +324,57 @@ class DeviceBench:
             pass
 
 
+class Pipe:
+    """Pipelined stepping from page-locked host memory (glint_pipe_*): the
+    next step's points are copied while the current step computes, and each
+    step's meetings land in page-locked result buffers.  submit(points, t)
+    finishes the step before; result(t) gives (stats, meetings) of the last
+    finished step, a view valid until the submit two steps later."""
+
+    def __init__(self, bench: DeviceBench, result_capacity: int = 0):
+        self.lib = bench.lib
+        self.bench = bench
+        h = ctypes.c_void_p()
+        st = self.lib.glint_pipe_create(bench.h, int(result_capacity), ctypes.byref(h))
+        if st != 0:
+            raise GlintError(st, bench.last_error())
+        self.h = h
+        self._keep = [None, None]
+
+    def submit(self, points, cur_time: int):
+        """points: an (N, 2) float64 array, ideally from pinned_empty (other
+        memory is copied synchronously by the driver)."""
+        p = np.ascontiguousarray(points, dtype=np.float64)
+        st = self.lib.glint_pipe_submit(self.h, p.ctypes.data_as(ctypes.c_void_p), int(cur_time))
+        if st != 0:
+            raise GlintError(st, self.bench.last_error())
+        self._keep = [self._keep[1], p]
+
+    def result(self, cur_time: int):
+        stats = GlintStepStats()
+        ptr = ctypes.c_void_p()
+        n = ctypes.c_uint64()
+        st = self.lib.glint_pipe_result(self.h, int(cur_time), ctypes.byref(stats), ctypes.byref(ptr),
+                                        ctypes.byref(n))
+        if st != 0:
+            raise GlintError(st, self.bench.last_error())
+        if n.value == 0:
+            return stats, np.zeros(0, MEETING_DTYPE)
+        raw = (ctypes.c_uint8 * (MEETING_DTYPE.itemsize * n.value)).from_address(ptr.value)
+        return stats, np.frombuffer(raw, dtype=MEETING_DTYPE)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.glint_pipe_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class Server:
     """Continuous-batching query server over a DeviceBench's kept store blocks
     (glint_server_*)."""

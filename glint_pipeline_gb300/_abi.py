@@ -219,6 +219,11 @@ def load_library(path: str | None = None):
     lib.glint_store_file_error.restype = ctypes.c_char_p
     lib.glint_store_dump.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
     lib.glint_store_load.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
+    lib.glint_pipe_create.argtypes = [vp, u64, ctypes.POINTER(vp)]
+    lib.glint_pipe_destroy.argtypes = [vp]
+    lib.glint_pipe_submit.argtypes = [vp, vp, u32]
+    lib.glint_pipe_result.argtypes = [vp, u32, ctypes.POINTER(GlintStepStats), ctypes.POINTER(vp),
+                                      ctypes.POINTER(u64)]
     lib.glint_host_alloc.argtypes = [ctypes.c_size_t, ctypes.POINTER(vp)]
     lib.glint_host_free.argtypes = [vp]
     lib.glint_precision_probe.argtypes = [vp, u32, ctypes.POINTER(GlintPrecisionReport)]

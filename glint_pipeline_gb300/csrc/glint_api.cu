@@ -590,7 +590,8 @@ static void launch_step(glint_ctx *c, const double *points, bool host) {
     cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, s);
 }
 
-static glint_status enqueue_step(glint_ctx *c, const double *points, bool host, uint32_t cur_time) {
+static glint_status enqueue_step(glint_ctx *c, const double *points, bool host, uint32_t cur_time,
+                                 bool allow_graph = true) {
     cudaStream_t s = c->stream;
     /* a captured step reads its parameters from host memory when it runs:
      * the previous step must have finished before they are overwritten */
@@ -601,7 +602,7 @@ static glint_status enqueue_step(glint_ctx *c, const double *points, bool host, 
     c->h_params->step_tag = stamp_of(c->step_index);
     c->h_params->end_time_min = c->end_time_min;
     c->stats_valid = false;
-    if (!c->cfg.use_graph || host) {
+    if (!c->cfg.use_graph || host || !allow_graph) {
         launch_step(c, points, host);
     } else {
         if (c->graph_exec && c->graph_src != (const void *)points) {
@@ -809,3 +810,11 @@ glint_status glint_get_buckets(glint_ctx *c, uint64_t *keys, uint32_t *starts, f
 }
 
 } /* extern "C" */
+
+namespace glint {
+/* the step on device points, never through the captured graph (whose input
+ * buffer is fixed) */
+glint_status enqueue_device_step_plain(glint_ctx *c, const double *d_points, uint32_t cur_time) {
+    return enqueue_step(c, d_points, false, cur_time, false);
+}
+} // namespace glint

@@ -118,6 +118,8 @@ struct StepTimers {
     bool created = false;
 };
 
+glint_status enqueue_device_step_plain(glint_ctx *c, const double *d_points, uint32_t cur_time);
+
 } // namespace glint
 
 struct glint_ctx {

@@ -216,6 +216,29 @@ glint_status glint_get_capacities(const glint_ctx *ctx, uint32_t *schema_capacit
 /* the context's cudaStream_t */
 void *glint_stream(glint_ctx *ctx);
 
+/* ---- pipelined stepping from host memory ----------------------------------
+ * No counterpart in the reference, whose process_with_gpu copies the points
+ * in and the results out around each step (cuda/geometry.cu:1625,
+ * 2142-2157).  glint_pipe_submit starts copying a step's points (page-locked
+ * memory, glint_host_alloc) on a copy stream into the second of two device
+ * buffers while the step before computes, then finishes that step (its
+ * statistics and, with auto_flush, its flush, so the flush still falls
+ * between the two steps) and queues the new one.  At the end of each step a
+ * kernel writes its meetings straight into one of two page-locked result
+ * buffers of result_capacity records (0: num_objects).  glint_pipe_result
+ * returns a step's statistics and meetings (waiting for it if it is still in
+ * flight); they stay valid until the submit two steps later, and only the
+ * last finished step can be asked for.  GLINT_ERR_CAPACITY when a step had
+ * more meetings than result_capacity (the first result_capacity are there;
+ * glint_meetings reads them all).  The context's own stepping calls must not
+ * be mixed in while a pipe has a step in flight. */
+typedef struct glint_pipe glint_pipe;
+glint_status glint_pipe_create(glint_ctx *ctx, uint64_t result_capacity, glint_pipe **out);
+glint_status glint_pipe_destroy(glint_pipe *pipe);
+glint_status glint_pipe_submit(glint_pipe *pipe, const double *points, uint32_t cur_time);
+glint_status glint_pipe_result(glint_pipe *pipe, uint32_t cur_time, glint_step_stats *stats,
+                               const glint_meeting **meetings, uint64_t *n);
+
 /* Page-locked host memory (cudaMallocHost) for step inputs and results:
  * glint_step's copy of the points and glint_meetings' copy of the meetings
  * run at the full host link rate from and into it, where pageable memory is

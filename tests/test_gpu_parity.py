@@ -299,3 +299,43 @@ def test_meetings_into_pinned_buffer():
         assert seen > 0
     finally:
         g.close()
+
+
+def test_pipelined_stepping_matches_plain_steps():
+    """glint_pipe_*: with the next step's points copied while the current
+    step runs and meetings written into page-locked result buffers, every
+    step's meetings and counts, the automatic flushes in between and the
+    final store equal those of plain glint_step calls."""
+    from glint_pipeline_gb300 import Pipe, pinned_empty
+    name = "dense_20k"
+    box, pts = make_points(name, 36)
+    cfgd = case_config(name)
+    n = cfgd["num_objects"]
+    kw = dict(precision_mode=1, auto_flush=True, kv_restriction=3000, kv_capacity=1 << 20, store_keep=2)
+    a = DeviceBench(gpu_config(cfgd, **kw), box, pts[0])
+    b = DeviceBench(gpu_config(cfgd, **kw), box, pts[0])
+    host = pinned_empty((pts.shape[0], n, 2), np.float64)
+    host[:] = pts
+    pipe = Pipe(b, result_capacity=n)
+    try:
+        pipe.submit(host[0], 0)
+        flushes = 0
+        for t in range(pts.shape[0]):
+            sa = a.step(pts[t], t)
+            ma = a.meetings()
+            if t + 1 < pts.shape[0]:
+                pipe.submit(host[t + 1], t + 1)
+            sb, mb = pipe.result(t)
+            assert sb.cur_time == t
+            assert (sa.contacts, sa.new_keys, sa.meetings, sa.flushed, sa.kv_count) == \
+                   (sb.contacts, sb.new_keys, sb.meetings, sb.flushed, sb.kv_count), t
+            np.testing.assert_array_equal(ma.view(np.uint8), mb.view(np.uint8), err_msg=f"step {t}")
+            flushes += sa.flushed
+        assert flushes >= 2
+        sa_, sb_ = a.store(), b.store()
+        for k in ("keys", "sids", "ctfs", "bitmaps", "o_keys"):
+            np.testing.assert_array_equal(sa_[k], sb_[k], err_msg=k)
+    finally:
+        pipe.close()
+        a.close()
+        b.close()
