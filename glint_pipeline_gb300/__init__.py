@@ -324,6 +324,51 @@ class DeviceBench:
             pass
 
 
+class TraceFiles:
+    """The reference's trace chunk files (<prefix><st>_<N>.tr, 100 steps
+    each), read ahead on a host thread into page-locked step buffers
+    (glint_trace_*).  step(t) returns an (N, 2) view valid until two more
+    steps have been asked for."""
+
+    def __init__(self, prefix: str, num_objects: int, first_step: int, num_steps: int, ring: int = 4):
+        self.lib = _abi.lib()
+        self.n = int(num_objects)
+        h = ctypes.c_void_p()
+        st = self.lib.glint_trace_open(prefix.encode(), self.n, int(first_step), int(num_steps), int(ring),
+                                       ctypes.byref(h))
+        if st != 0:
+            raise GlintError(st, self.lib.glint_trace_error().decode())
+        self.h = h
+
+    def step(self, t: int) -> np.ndarray:
+        ptr = ctypes.c_void_p()
+        st = self.lib.glint_trace_step(self.h, int(t), ctypes.byref(ptr))
+        if st != 0:
+            raise GlintError(st, self.lib.glint_trace_error().decode())
+        raw = (ctypes.c_double * (2 * self.n)).from_address(ptr.value)
+        return np.frombuffer(raw, dtype=np.float64).reshape(self.n, 2)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.glint_trace_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def write_trace_files(prefix: str, first_step: int, points: np.ndarray):
+    """steps of points (steps, N, 2) into the reference's chunk files"""
+    p = np.ascontiguousarray(points, dtype=np.float64)
+    lib = _abi.lib()
+    st = lib.glint_trace_write(prefix.encode(), int(p.shape[1]), int(first_step), p.ctypes.data, int(p.shape[0]))
+    if st != 0:
+        raise GlintError(st, lib.glint_trace_error().decode())
+
+
 class Pipe:
     """Pipelined stepping from page-locked host memory (glint_pipe_*): the
     next step's points are copied while the current step computes, and each

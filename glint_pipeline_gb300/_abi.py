@@ -219,6 +219,11 @@ def load_library(path: str | None = None):
     lib.glint_store_file_error.restype = ctypes.c_char_p
     lib.glint_store_dump.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
     lib.glint_store_load.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
+    lib.glint_trace_open.argtypes = [ctypes.c_char_p, u32, u32, u32, u32, ctypes.POINTER(vp)]
+    lib.glint_trace_step.argtypes = [vp, u32, ctypes.POINTER(vp)]
+    lib.glint_trace_close.argtypes = [vp]
+    lib.glint_trace_error.restype = ctypes.c_char_p
+    lib.glint_trace_write.argtypes = [ctypes.c_char_p, u32, u32, vp, u32]
     lib.glint_pipe_create.argtypes = [vp, u64, ctypes.POINTER(vp)]
     lib.glint_pipe_destroy.argtypes = [vp]
     lib.glint_pipe_submit.argtypes = [vp, vp, u32]

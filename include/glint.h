@@ -216,6 +216,29 @@ glint_status glint_get_capacities(const glint_ctx *ctx, uint32_t *schema_capacit
 /* the context's cudaStream_t */
 void *glint_stream(glint_ctx *ctx);
 
+/* ---- the reference's trace files ------------------------------------------
+ * A trace is stored as files <prefix><st>_<num_objects>.tr, st a multiple of
+ * 100, each holding 100 steps of num_objects (lon, lat) doubles, step after
+ * step, no header (tools/datagen.cpp:18-26, read by tracer::loadData,
+ * tracing/process.cpp:128-144).  glint_trace_open starts a host thread that
+ * reads steps [first_step, first_step + num_steps) in order into a ring of
+ * `ring` (>= 3) page-locked step buffers ahead of the caller.
+ * glint_trace_step waits for step t and returns its points; the two steps
+ * most recently returned stay valid (the last may still be in an
+ * asynchronous copy such as glint_pipe_submit's), older ones are reused.
+ * Failures (a missing or short file) are reported by glint_trace_step, with
+ * the message in glint_trace_error. */
+typedef struct glint_trace glint_trace;
+glint_status glint_trace_open(const char *prefix, uint32_t num_objects, uint32_t first_step, uint32_t num_steps,
+                              uint32_t ring, glint_trace **out);
+glint_status glint_trace_step(glint_trace *trace, uint32_t t, const double **points);
+glint_status glint_trace_close(glint_trace *trace);
+const char *glint_trace_error(void);
+/* num_steps steps of points (step-major, num_objects (lon, lat) pairs each)
+ * from first_step on, into the chunk files of that layout */
+glint_status glint_trace_write(const char *prefix, uint32_t num_objects, uint32_t first_step, const double *points,
+                               uint32_t num_steps);
+
 /* ---- pipelined stepping from host memory ----------------------------------
  * No counterpart in the reference, whose process_with_gpu copies the points
  * in and the results out around each step (cuda/geometry.cu:1625,

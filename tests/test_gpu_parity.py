@@ -339,3 +339,38 @@ def test_pipelined_stepping_matches_plain_steps():
         pipe.close()
         a.close()
         b.close()
+
+
+def test_trace_files_through_pipe_match_oracle(tmp_path):
+    """The reference's trace chunk files, read ahead by glint_trace_* and fed
+    to glint_pipe_*, give the oracle's meetings step by step, across a chunk
+    boundary."""
+    from glint_pipeline_gb300 import Pipe, TraceFiles, write_trace_files
+    name = "dense_20k"
+    box, pts = make_points(name, 130)
+    cfgd = case_config(name)
+    n = cfgd["num_objects"]
+    prefix = str(tmp_path / "trace_")
+    write_trace_files(prefix, 0, pts)
+    o = Oracle(make_config(**cfgd), box, pts[0])
+    g = DeviceBench(gpu_config(cfgd, precision_mode=1), box, pts[0])
+    tr = TraceFiles(prefix, n, 80, 40)
+    pipe = Pipe(g)
+    try:
+        for t in range(80):
+            o.step(pts[t], t)
+            g.step(pts[t], t)
+        pipe.submit(tr.step(80), 80)
+        for t in range(80, 120):
+            o.step(pts[t], t)
+            if t + 1 < 120:
+                pipe.submit(tr.step(t + 1), t + 1)
+            st, m = pipe.result(t)
+            c = o.counts()
+            assert (st.candidates, st.contacts) == (c.candidates, c.contacts), t
+            compare_meetings(o.meetings(), m, t)
+    finally:
+        pipe.close()
+        tr.close()
+        g.close()
+        o.close()
