@@ -297,6 +297,25 @@ class DeviceBench:
     def last_error(self) -> str:
         return self.lib.glint_last_error(self.h).decode()
 
+    def snapshot(self, path: str):
+        """Everything the next steps read, into one file (glint_snapshot_save)."""
+        st = self.lib.glint_snapshot_save(self.h, path.encode())
+        if st != 0:
+            raise GlintError(st, self.last_error())
+
+    @classmethod
+    def resume(cls, path: str, config: Configuration, device: int = -1) -> "DeviceBench":
+        """A context that continues from a snapshot (glint_snapshot_load);
+        `config` is the configuration the snapshot was taken with."""
+        lib = _abi.lib()
+        h = ctypes.c_void_p()
+        st = lib.glint_snapshot_load(path.encode(), int(device), ctypes.byref(h))
+        if st != 0:
+            raise GlintError(st, "glint_snapshot_load")
+        b = cls._view(h.value, config)
+        b._owned = True
+        return b
+
     @classmethod
     def _view(cls, handle: int, config: Configuration):
         """A DeviceBench over a context owned elsewhere (a batch region)."""

@@ -219,6 +219,8 @@ def load_library(path: str | None = None):
     lib.glint_store_file_error.restype = ctypes.c_char_p
     lib.glint_store_dump.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
     lib.glint_store_load.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
+    lib.glint_snapshot_save.argtypes = [vp, ctypes.c_char_p]
+    lib.glint_snapshot_load.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(vp)]
     lib.glint_trace_open.argtypes = [ctypes.c_char_p, u32, u32, u32, u32, ctypes.POINTER(vp)]
     lib.glint_trace_step.argtypes = [vp, u32, ctypes.POINTER(vp)]
     lib.glint_trace_close.argtypes = [vp]

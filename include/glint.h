@@ -216,6 +216,19 @@ glint_status glint_get_capacities(const glint_ctx *ctx, uint32_t *schema_capacit
 /* the context's cudaStream_t */
 void *glint_stream(glint_ctx *ctx);
 
+/* ---- snapshot and resume -------------------------------------------------
+ * The reference's workbench::dump_meta / load_meta (tracing/workbench.cpp:
+ * 574-596, tracing/process.cpp:213-236) keep the flushed blocks but not the
+ * meetings in progress.  glint_snapshot_save writes, between steps, all the
+ * state the next steps read: configuration, schema and free stacks, the
+ * occupied buckets of the meeting table, the pending keys of the current
+ * window, the last step's meetings, the last flushed store, the kept blocks
+ * and the counters.  glint_snapshot_load creates a context from such a file
+ * (on `device`, or the saved one when negative) that continues bit for bit
+ * as the saved context would. */
+glint_status glint_snapshot_save(glint_ctx *ctx, const char *path);
+glint_status glint_snapshot_load(const char *path, int device, glint_ctx **out);
+
 /* ---- the reference's trace files ------------------------------------------
  * A trace is stored as files <prefix><st>_<num_objects>.tr, st a multiple of
  * 100, each holding 100 steps of num_objects (lon, lat) doubles, step after

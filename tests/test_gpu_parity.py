@@ -374,3 +374,53 @@ def test_trace_files_through_pipe_match_oracle(tmp_path):
         tr.close()
         g.close()
         o.close()
+
+
+def test_snapshot_resume_continues_bit_for_bit(tmp_path):
+    """glint_snapshot_save between steps and glint_snapshot_load in a new
+    context: the resumed context's next steps give the same meetings, counts,
+    flushes, schema, bucket table, store and query answers as the saved
+    context's own next steps."""
+    name = "dense_20k"
+    box, pts = make_points(name, 50)
+    cfgd = case_config(name)
+    cfg = gpu_config(cfgd, precision_mode=1, auto_flush=True, kv_restriction=3000, kv_capacity=1 << 20,
+                     store_keep=3)
+    a = DeviceBench(cfg, box, pts[0])
+    b = None
+    try:
+        for t in range(30):
+            a.step(pts[t], t)
+        path = str(tmp_path / "ctx.snap")
+        a.snapshot(path)
+        b = DeviceBench.resume(path, cfg)
+        np.testing.assert_array_equal(a.meetings().view(np.uint8), b.meetings().view(np.uint8))
+        flushes = 0
+        for t in range(30, 50):
+            sa, sb = a.step(pts[t], t), b.step(pts[t], t)
+            assert (sa.candidates, sa.contacts, sa.new_keys, sa.meetings, sa.flushed, sa.kv_count, sa.leaves,
+                    sa.nodes) == (sb.candidates, sb.contacts, sb.new_keys, sb.meetings, sb.flushed, sb.kv_count,
+                                  sb.leaves, sb.nodes), t
+            np.testing.assert_array_equal(a.meetings().view(np.uint8), b.meetings().view(np.uint8), err_msg=str(t))
+            flushes += sa.flushed
+        assert flushes >= 1
+        for x, y in zip(a.schema(), b.schema()):
+            np.testing.assert_array_equal(np.asarray(x), np.asarray(y))
+        (ka, sa_start, ma), (kb, sb_start, mb) = a.buckets(), b.buckets()
+        np.testing.assert_array_equal(ka, kb)
+        occupied = ka != (1 << 62)
+        np.testing.assert_array_equal(sa_start[occupied], sb_start[occupied])
+        np.testing.assert_array_equal(ma[occupied].view(np.uint32), mb[occupied].view(np.uint32))
+        sa_, sb_ = a.store(), b.store()
+        for k in ("keys", "sids", "ctfs", "bitmaps", "o_keys", "o_boxes", "o_bitmap"):
+            np.testing.assert_array_equal(sa_[k], sb_[k], err_msg=k)
+        assert a.store_blocks() == b.store_blocks() == 3
+        rng = np.random.default_rng(5)
+        qs = [(rng.choice(cfgd["num_objects"], 200, replace=False).astype(np.uint32), 2, 0, 0)]
+        ra, rb = a.query(qs), b.query(qs)
+        for h in range(2):
+            np.testing.assert_array_equal(ra[0][0][h], rb[0][0][h])
+    finally:
+        if b is not None:
+            b.close()
+        a.close()
