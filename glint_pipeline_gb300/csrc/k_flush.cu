@@ -258,6 +258,53 @@ __global__ void k_key_scatter(const u128 *__restrict__ keys, const float4 *__res
 
 __device__ inline bool u128_less(u128 a, u128 b) { return a < b; }
 
+constexpr uint32_t kSegTinyMax = 8;
+
+/* segments of 2..8 keys, one thread each: the 19-comparator sorting network
+ * for eight elements over (key, box), padded with the largest key */
+__global__ void __launch_bounds__(256) k_seg_sort_tiny(const unsigned long long *__restrict__ gk,
+                                                       const uint32_t *__restrict__ gv,
+                                                       const uint32_t *__restrict__ start,
+                                                       const uint32_t *__restrict__ same, uint32_t N,
+                                                       u128 *__restrict__ keys, float4 *__restrict__ boxes) {
+    for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < N; g += gridDim.x * blockDim.x) {
+        if (gk[g] == kGroupNone) continue;
+        const uint32_t n = same[gv[g]];
+        if (n <= 1 || n > kSegTinyMax) continue;
+        const uint32_t b = start[g];
+        u128 k[kSegTinyMax];
+        float4 x[kSegTinyMax];
+#pragma unroll
+        for (uint32_t i = 0; i < kSegTinyMax; ++i) {
+            k[i] = i < n ? keys[b + i] : ~(u128)0;
+            x[i] = i < n ? boxes[b + i] : make_float4(0, 0, 0, 0);
+        }
+#define GLINT_CE(i, j)                   \
+    if (k[j] < k[i]) {                   \
+        const u128 tk = k[i];            \
+        k[i] = k[j];                     \
+        k[j] = tk;                       \
+        const float4 tx = x[i];          \
+        x[i] = x[j];                     \
+        x[j] = tx;                       \
+    }
+        GLINT_CE(0, 1) GLINT_CE(2, 3) GLINT_CE(4, 5) GLINT_CE(6, 7)
+        GLINT_CE(0, 2) GLINT_CE(1, 3) GLINT_CE(4, 6) GLINT_CE(5, 7)
+        GLINT_CE(1, 2) GLINT_CE(5, 6) GLINT_CE(0, 4) GLINT_CE(3, 7)
+        GLINT_CE(1, 5) GLINT_CE(2, 6)
+        GLINT_CE(1, 4) GLINT_CE(3, 6)
+        GLINT_CE(2, 4) GLINT_CE(3, 5)
+        GLINT_CE(3, 4)
+#undef GLINT_CE
+#pragma unroll
+        for (uint32_t i = 0; i < kSegTinyMax; ++i)
+            if (i < n) {
+                keys[b + i] = k[i];
+                boxes[b + i] = x[i];
+            }
+    }
+}
+
 /* one warp sorts segments of up to kSegWarpMax keys: in registers up to 32,
  * else a shared-memory bitonic sort of (key, index) */
 __global__ void __launch_bounds__(128) k_seg_sort_warp(const unsigned long long *__restrict__ gk,
@@ -273,7 +320,7 @@ __global__ void __launch_bounds__(128) k_seg_sort_warp(const unsigned long long 
     for (uint32_t g = blockIdx.x * 4 + w; g < N; g += gridDim.x * 4) {
         if (gk[g] == kGroupNone) continue;
         const uint32_t n = same[gv[g]];
-        if (n <= 1) continue;
+        if (n <= kSegTinyMax) continue; /* k_seg_sort_tiny */
         const uint32_t b = start[g];
         if (n > kSegWarpMax) {
             if (lane == 0) big[atomicAdd(n_big, 1u)] = g;
@@ -402,17 +449,25 @@ __global__ void __launch_bounds__(1024) k_seg_sort_block(const uint32_t *__restr
     }
 }
 
-/* get_CTF_capacity (:808-818) */
-__global__ void k_ctf_capacity(const uint32_t *__restrict__ oids, uint32_t N, uint32_t zero_one,
-                               const uint16_t *__restrict__ sids, const uint32_t *__restrict__ same, uint32_t C,
-                               uint32_t *__restrict__ cap, DevCounters *cnt) {
+/* get_CTF_capacity (:808-818); the C counters are summed per block in
+ * shared memory first (C <= 4096) */
+__global__ void __launch_bounds__(256) k_ctf_capacity(const uint32_t *__restrict__ oids, uint32_t N,
+                                                      uint32_t zero_one, const uint16_t *__restrict__ sids,
+                                                      const uint32_t *__restrict__ same, uint32_t C,
+                                                      uint32_t *__restrict__ cap, DevCounters *cnt) {
+    __shared__ uint32_t part[4096];
+    for (uint32_t i = threadIdx.x; i < C; i += blockDim.x) part[i] = 0;
+    __syncthreads();
     for (uint32_t id = blockIdx.x * blockDim.x + threadIdx.x; id < N; id += gridDim.x * blockDim.x) {
         if (id < zero_one) continue;
         const uint32_t oid = oids[id];
         const uint32_t c = (uint32_t)sids[oid] - 2u;
-        if (c < C) atomicAdd(&cap[c], same[oid]);
+        if (c < C) atomicAdd(&part[c], same[oid]);
         else atomicOr(&cnt->error_flags, GLINT_EF_STORE_DOMAIN);
     }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < C; i += blockDim.x)
+        if (part[i]) atomicAdd(&cap[i], part[i]);
 }
 
 /* the reductions of cuda_get_limit (:820-906) / get_o_limit (:928-1000) over
@@ -472,8 +527,14 @@ __global__ void __launch_bounds__(1024) k_limits(const u128 *__restrict__ keys, 
 }
 
 __device__ inline void set_bit_global(uint32_t *bits, uint64_t total, uint64_t pos, unsigned long long *outside) {
-    if (pos < total) atomicOr(&bits[pos >> 5], 1u << (pos & 31));
-    else atomicAdd(outside, 1ull);
+    if (pos < total) {
+        /* many keys set the same bits: bits only go from 0 to 1 here, so a
+         * bit already seen set (read at L2) needs no atomic */
+        const uint32_t m = 1u << (pos & 31);
+        if (!(__ldcg(&bits[pos >> 5]) & m)) atomicOr(&bits[pos >> 5], m);
+    } else {
+        atomicAdd(outside, 1ull);
+    }
 }
 
 /* bits x + y * row for x in [l0, h0], y in [l1, h1] from `base`, inside
@@ -784,6 +845,7 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
     std::swap(c->d_keys, c->d_keys2);
     std::swap(c->d_kvbox, c->d_kvbox2);
     u128 *keys = reinterpret_cast<u128 *>(c->d_keys);
+    k_seg_sort_tiny<<<grid_for(N, 256), 256, 0, s>>>(gk, gv, c->d_gstart, c->d_same, N, keys, c->d_kvbox);
     k_seg_sort_warp<<<152 * 8, 128, 0, s>>>(gk, gv, c->d_gstart, c->d_same, N, keys, c->d_kvbox, c->d_segbig,
                                            d_nbig);
     k_seg_sort_block<<<152, 1024, kSegBlockMax * (sizeof(u128) + sizeof(uint32_t)), s>>>(
@@ -791,7 +853,7 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
 
     /* CTF capacities, then the part sizes on the host */
     cudaMemsetAsync(c->d_ctf_cap, 0, sizeof(uint32_t) * C, s);
-    k_ctf_capacity<<<grid_for(N, 256), 256, 0, s>>>(c->d_oids, N, zero_one, c->d_sids, c->d_same, C, c->d_ctf_cap,
+    k_ctf_capacity<<<grid_for(N, 256, 152u * 8u), 256, 0, s>>>(c->d_oids, N, zero_one, c->d_sids, c->d_same, C, c->d_ctf_cap,
                                                     c->d_cnt);
     std::vector<uint32_t> cap(C);
     unsigned long long kv = 0;
