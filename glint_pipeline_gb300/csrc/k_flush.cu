@@ -259,6 +259,7 @@ __global__ void k_key_scatter(const u128 *__restrict__ keys, const float4 *__res
 __device__ inline bool u128_less(u128 a, u128 b) { return a < b; }
 
 constexpr uint32_t kSegTinyMax = 8;
+constexpr uint32_t kSegHalfMax = 16;
 
 /* segments of 2..8 keys, one thread each: the 19-comparator sorting network
  * for eight elements over (key, box), padded with the largest key */
@@ -266,10 +267,20 @@ __global__ void __launch_bounds__(256) k_seg_sort_tiny(const unsigned long long 
                                                        const uint32_t *__restrict__ gv,
                                                        const uint32_t *__restrict__ start,
                                                        const uint32_t *__restrict__ same, uint32_t N,
-                                                       u128 *__restrict__ keys, float4 *__restrict__ boxes) {
+                                                       u128 *__restrict__ keys, float4 *__restrict__ boxes,
+                                                       uint32_t *__restrict__ mid, unsigned int *n_mid,
+                                                       uint32_t *__restrict__ large, unsigned int *n_large) {
     for (uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < N; g += gridDim.x * blockDim.x) {
         if (gk[g] == kGroupNone) continue;
         const uint32_t n = same[gv[g]];
+        if (n > kSegTinyMax && n <= kSegHalfMax) {
+            mid[atomicAdd(n_mid, 1u)] = g; /* k_seg_sort_half */
+            continue;
+        }
+        if (n > kSegHalfMax) {
+            large[atomicAdd(n_large, 1u)] = g; /* k_seg_sort_warp */
+            continue;
+        }
         if (n <= 1 || n > kSegTinyMax) continue;
         const uint32_t b = start[g];
         u128 k[kSegTinyMax];
@@ -305,22 +316,74 @@ __global__ void __launch_bounds__(256) k_seg_sort_tiny(const unsigned long long 
     }
 }
 
-/* one warp sorts segments of up to kSegWarpMax keys: in registers up to 32,
- * else a shared-memory bitonic sort of (key, index) */
-__global__ void __launch_bounds__(128) k_seg_sort_warp(const unsigned long long *__restrict__ gk,
+/* segments of 9..16 keys, two per warp: a 16-lane bitonic sort in registers
+ * (the shuffles stay inside each half of the warp) */
+__global__ void __launch_bounds__(128) k_seg_sort_half(const uint32_t *__restrict__ mid,
+                                                       const unsigned int *__restrict__ n_mid,
                                                        const uint32_t *__restrict__ gv,
                                                        const uint32_t *__restrict__ start,
-                                                       const uint32_t *__restrict__ same, uint32_t N,
+                                                       const uint32_t *__restrict__ same, u128 *__restrict__ keys,
+                                                       float4 *__restrict__ boxes) {
+    const int lane = threadIdx.x & 31, half = lane >> 4, hl = lane & 15;
+    const uint32_t total = *n_mid;
+    const uint32_t warps = gridDim.x * (blockDim.x >> 5);
+    for (uint32_t p = (blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)) * 2; p < total; p += 2 * warps) {
+        const uint32_t i = p + half;
+        uint32_t n = 0, b = 0;
+        if (i < total) {
+            const uint32_t g = mid[i];
+            n = same[gv[g]];
+            b = start[g];
+        }
+        u128 k = ~(u128)0;
+        float4 bx = make_float4(0, 0, 0, 0);
+        if ((uint32_t)hl < n) {
+            k = keys[b + hl];
+            bx = boxes[b + hl];
+        }
+        for (int kk = 2; kk <= 16; kk <<= 1) {
+            for (int j = kk >> 1; j > 0; j >>= 1) {
+                const unsigned long long lo = (unsigned long long)k, hi = (unsigned long long)(k >> 64);
+                const unsigned long long olo = __shfl_xor_sync(0xffffffffu, lo, j);
+                const unsigned long long ohi = __shfl_xor_sync(0xffffffffu, hi, j);
+                const float4 ob = make_float4(__shfl_xor_sync(0xffffffffu, bx.x, j),
+                                              __shfl_xor_sync(0xffffffffu, bx.y, j),
+                                              __shfl_xor_sync(0xffffffffu, bx.z, j),
+                                              __shfl_xor_sync(0xffffffffu, bx.w, j));
+                const u128 o = ((u128)ohi << 64) | olo;
+                const bool up = (hl & kk) == 0;
+                const bool lower = (hl & j) == 0;
+                const bool take_min = lower == up;
+                if (take_min ? (o < k) : (k < o)) {
+                    k = o;
+                    bx = ob;
+                }
+            }
+        }
+        if ((uint32_t)hl < n) {
+            keys[b + hl] = k;
+            boxes[b + hl] = bx;
+        }
+    }
+}
+
+/* one warp sorts segments of up to kSegWarpMax keys: in registers up to 32,
+ * else a shared-memory bitonic sort of (key, index) */
+__global__ void __launch_bounds__(128) k_seg_sort_warp(const uint32_t *__restrict__ large,
+                                                       const unsigned int *__restrict__ n_large,
+                                                       const uint32_t *__restrict__ gv,
+                                                       const uint32_t *__restrict__ start,
+                                                       const uint32_t *__restrict__ same,
                                                        u128 *__restrict__ keys, float4 *__restrict__ boxes,
                                                        uint32_t *__restrict__ big, unsigned int *n_big) {
     __shared__ u128 sk[4][kSegWarpMax];
     __shared__ uint16_t si[4][kSegWarpMax];
     __shared__ float4 sb[4][kSegWarpMax];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    for (uint32_t g = blockIdx.x * 4 + w; g < N; g += gridDim.x * 4) {
-        if (gk[g] == kGroupNone) continue;
+    const uint32_t total = *n_large;
+    for (uint32_t li = blockIdx.x * 4 + w; li < total; li += gridDim.x * 4) {
+        const uint32_t g = large[li];
         const uint32_t n = same[gv[g]];
-        if (n <= kSegTinyMax) continue; /* k_seg_sort_tiny */
         const uint32_t b = start[g];
         if (n > kSegWarpMax) {
             if (lane == 0) big[atomicAdd(n_big, 1u)] = g;
@@ -845,9 +908,17 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
     std::swap(c->d_keys, c->d_keys2);
     std::swap(c->d_kvbox, c->d_kvbox2);
     u128 *keys = reinterpret_cast<u128 *>(c->d_keys);
-    k_seg_sort_tiny<<<grid_for(N, 256), 256, 0, s>>>(gk, gv, c->d_gstart, c->d_same, N, keys, c->d_kvbox);
-    k_seg_sort_warp<<<152 * 8, 128, 0, s>>>(gk, gv, c->d_gstart, c->d_same, N, keys, c->d_kvbox, c->d_segbig,
-                                           d_nbig);
+    /* segments by size: up to 8 keys a thread each, 9..16 two per warp (the
+     * per-object cursors of the scatter are free again and list them), up
+     * to kSegWarpMax a warp each, longer ones a block each */
+    unsigned int *d_nmid = reinterpret_cast<unsigned int *>(c->d_fmisc + 3);
+    unsigned int *d_nlarge = reinterpret_cast<unsigned int *>(c->d_fmisc + 4);
+    uint32_t *d_large = reinterpret_cast<uint32_t *>(c->d_mid2); /* the group sort's scratch, free again */
+    k_seg_sort_tiny<<<grid_for(N, 256), 256, 0, s>>>(gk, gv, c->d_gstart, c->d_same, N, keys, c->d_kvbox,
+                                                     c->d_segcur, d_nmid, d_large, d_nlarge);
+    k_seg_sort_half<<<152 * 8, 128, 0, s>>>(c->d_segcur, d_nmid, gv, c->d_gstart, c->d_same, keys, c->d_kvbox);
+    k_seg_sort_warp<<<152 * 8, 128, 0, s>>>(d_large, d_nlarge, gv, c->d_gstart, c->d_same, keys, c->d_kvbox,
+                                           c->d_segbig, d_nbig);
     k_seg_sort_block<<<152, 1024, kSegBlockMax * (sizeof(u128) + sizeof(uint32_t)), s>>>(
         c->d_segbig, gv, c->d_gstart, c->d_same, keys, c->d_kvbox, c->d_kvbox2, c->d_cnt, d_nbig);
 
