@@ -69,6 +69,7 @@ def parse():
     p.add_argument("--skew-objects", type=int, default=50_000_000)
     p.add_argument("--skew-buckets", type=int, default=1 << 31)
     p.add_argument("--core-objects", type=int, default=2_000_000)
+    p.add_argument("--core-buckets", type=int, default=0, help="0: 256 per object, rounded up to a power of two")
     return p.parse_args()
 
 
@@ -638,7 +639,7 @@ def run_skew(args, local):
     rt.cudaSetDevice(local)
     K, W = args.steps, max(args.warmup, 3)
     cases = [("spread", args.skew_objects, SKEW_SIGMA_SPREAD, args.skew_buckets, 256),
-             ("core", args.core_objects, 50.0, next_pow2(256 * args.core_objects), 16)]
+             ("core", args.core_objects, 50.0, args.core_buckets or next_pow2(256 * args.core_objects), 16)]
     out = {}
     for name, N, sigma, B, stride in cases:
         gen = TraceGenerator(SEED_SKEW, N, 1, sigma_m=sigma)

@@ -178,7 +178,7 @@ void free_all(glint_ctx *c) {
                     c->d_nodes, c->d_low, c->d_sstack, c->d_gstack, c->d_split, c->d_evscan, c->d_cand, c->d_newgid,
                     c->d_events, c->d_evpos, c->d_evlist, c->d_evdata, c->d_evlevel, c->d_big, c->d_qcount,
                     c->d_qstart, c->d_qlist, c->d_qtmp, c->d_tcount, c->d_tstart, c->d_tcursor, c->d_tlist, c->d_tab,
-                    c->d_stamp, c->d_newline, c->d_new, c->d_tile_cnt, c->d_tile_off, c->d_log, c->d_cnt, c->d_coef,
+                    c->d_stamp, c->d_newline, c->d_new, c->d_rextra, c->d_tile_cnt, c->d_tile_off, c->d_log, c->d_cnt, c->d_coef,
                     c->d_scan_tmp, c->d_qbits, c->d_qpids, c->d_qout, c->d_qn};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -411,6 +411,9 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     ALLOC(c->d_stamp, stamp_bytes(c->B));
     ALLOC(c->d_newline, newline_words(c->B));
     ALLOC(c->d_new, c->new_cap);
+    /* each extra refine item is a further kCrossChunk checks of one leaf */
+    c->rextra_cap = c->check_cap / kCrossChunk + 1;
+    ALLOC(c->d_rextra, c->rextra_cap);
     ALLOC(c->d_tile_cnt, c->n_tiles + 1);
     ALLOC(c->d_tile_off, c->n_tiles + 1);
     ALLOC(c->d_log, c->log_cap);

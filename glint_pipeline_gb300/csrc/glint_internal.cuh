@@ -54,7 +54,8 @@ struct DevCounters {
     unsigned int n_cand;                   /* merge candidates this step */
     unsigned int total_checks;
     unsigned int n_big;                    /* leaf segments sorted by a whole block */
-    unsigned int pad[2];
+    unsigned int n_extra;                  /* refine work items beyond each leaf's first */
+    unsigned int extra_next;               /* their scheduling cursor */
     /* persistent (not cleared per step) */
     unsigned int ssi;                      /* schema_stack_index */
     unsigned int gsi;                      /* grids_stack_index */
@@ -77,6 +78,9 @@ struct StepParams {
 };
 /* bytes cleared at the start of every step */
 constexpr size_t kStepCounterBytes = offsetof(DevCounters, ssi);
+
+/* cross-leaf checks per refine work item (refine_common.cuh) */
+constexpr uint32_t kCrossChunk = 64;
 
 struct NewEntry {
     unsigned long long key;
@@ -183,6 +187,8 @@ struct glint_ctx {
     uint8_t *d_stamp = nullptr;
     uint32_t *d_newline = nullptr;   /* one bit per 4 slots filled this step */
     glint::NewEntry *d_new = nullptr;
+    uint2 *d_rextra = nullptr;             /* refine work items (leaf, chunk of cross checks) */
+    uint64_t rextra_cap = 0;
     uint32_t *d_tile_cnt = nullptr, *d_tile_off = nullptr;
     uint64_t n_tiles = 0;
 

@@ -46,30 +46,32 @@ __global__ void __launch_bounds__(32 * kPrecWarps) k_refine_fp32(RefineArgs a) {
     unsigned long long cand = 0, hits = 0;
     uint32_t band = 0;
     uint32_t qn = 0;
-    const uint32_t nwork = a.cnt->n_leaf_work;
+    const uint32_t nwork = a.cnt->n_leaf_work, n_extra = a.cnt->n_extra;
     const uint32_t tag = a.cnt->step_tag;
+    bool extra_done = n_extra == 0;
+    uint32_t staged = ~0u;
     for (;;) {
-        uint32_t li = 0;
-        if (lane == 0) li = atomicAdd(&a.cnt->work_next, 1u);
-        li = __shfl_sync(0xffffffffu, li, 0);
-        if (li >= nwork) break;
-        const uint32_t g = a.work[li];
+        uint32_t g, chunk;
+        if (!claim_item(a, nwork, n_extra, extra_done, g, chunk)) break;
         const uint32_t s0 = a.grid_start[g];
         const uint32_t cnt_g = a.grid_count[g];
         const uint32_t k = cnt_g < cap ? cnt_g : cap;
-        for (uint32_t i = lane; i < k; i += 32) {
-            const longlong2 ip = a.sipos[s0 + i];
-            const float2 fp = a.sfpos[s0 + i];
-            sX[i] = ip.x;
-            sY[i] = ip.y;
-            sC[i] = a.sc[s0 + i];
-            sFx[i] = fp.x;
-            sFy[i] = fp.y;
-            sid[i] = a.sorted[s0 + i];
+        if (g != staged) {
+            for (uint32_t i = lane; i < k; i += 32) {
+                const longlong2 ip = a.sipos[s0 + i];
+                const float2 fp = a.sfpos[s0 + i];
+                sX[i] = ip.x;
+                sY[i] = ip.y;
+                sC[i] = a.sc[s0 + i];
+                sFx[i] = fp.x;
+                sFy[i] = fp.y;
+                sid[i] = a.sorted[s0 + i];
+            }
+            __syncwarp();
+            staged = g;
         }
-        __syncwarp();
         /* inside checks: p1 = member i, p2 = member j > i */
-        for (uint32_t i = 0; i + 1 < k; ++i) {
+        for (uint32_t i = 0; chunk == 0 && i + 1 < k; ++i) {
             const long long Xi = sX[i], Yi = sY[i];
             const float ci = sC[i];
             const uint32_t p1 = sid[i];
@@ -95,8 +97,10 @@ __global__ void __launch_bounds__(32 * kPrecWarps) k_refine_fp32(RefineArgs a) {
                         hit ? sFy[j] : 0.f, tag);
             }
         }
-        /* cross-leaf checks that target this leaf: p1 = the querier */
-        const uint32_t tb = a.tstart[g], te = a.tstart[g + 1];
+        /* cross-leaf checks that target this leaf, this item's chunk: p1 = the
+         * querier */
+        uint32_t tb, te;
+        item_checks(a, g, chunk, tb, te);
         for (uint32_t t = tb; t < te; ++t) {
             const uint2 qe = a.tlist[t];
             const uint32_t q = qe.x;

@@ -44,27 +44,29 @@ __global__ void __launch_bounds__(32 * kRefineWarps) k_refine_fp64(RefineArgs a)
 
     unsigned long long cand = 0, hits = 0;
     uint32_t qn = 0;
-    const uint32_t nwork = a.cnt->n_leaf_work;
+    const uint32_t nwork = a.cnt->n_leaf_work, n_extra = a.cnt->n_extra;
     const uint32_t tag = a.cnt->step_tag;
+    bool extra_done = n_extra == 0;
+    uint32_t staged = ~0u;
     for (;;) {
-        uint32_t li = 0;
-        if (lane == 0) li = atomicAdd(&a.cnt->work_next, 1u);
-        li = __shfl_sync(0xffffffffu, li, 0);
-        if (li >= nwork) break;
-        const uint32_t g = a.work[li];
+        uint32_t g, chunk;
+        if (!claim_item(a, nwork, n_extra, extra_done, g, chunk)) break;
         const uint32_t s0 = a.grid_start[g];
         const uint32_t cnt_g = a.grid_count[g];
         const uint32_t k = cnt_g < cap ? cnt_g : cap;
-        for (uint32_t i = lane; i < k; i += 32) {
-            const double2 p = a.sxy[s0 + i];
-            sx[i] = p.x;
-            sy[i] = p.y;
-            sLm[i] = a.sL[s0 + i];
-            sid[i] = a.sorted[s0 + i];
+        if (g != staged) {
+            for (uint32_t i = lane; i < k; i += 32) {
+                const double2 p = a.sxy[s0 + i];
+                sx[i] = p.x;
+                sy[i] = p.y;
+                sLm[i] = a.sL[s0 + i];
+                sid[i] = a.sorted[s0 + i];
+            }
+            __syncwarp();
+            staged = g;
         }
-        __syncwarp();
         /* inside checks: p1 = member i, p2 = member j > i (ids ascend with rank) */
-        for (uint32_t i = 0; i + 1 < k; ++i) {
+        for (uint32_t i = 0; chunk == 0 && i + 1 < k; ++i) {
             const double x1 = sx[i], y1 = sy[i], L1 = sLm[i];
             const uint32_t p1 = sid[i];
             const float fx1 = (float)x1, fy1 = (float)y1;
@@ -87,8 +89,9 @@ __global__ void __launch_bounds__(32 * kRefineWarps) k_refine_fp64(RefineArgs a)
                 enqueue(a, Q, qn, hit, pw, prio_pack(0, p1, 0, j), fx1, fy1, fx2, fy2, tag);
             }
         }
-        /* cross-leaf checks that target this leaf */
-        const uint32_t tb = a.tstart[g], te = a.tstart[g + 1];
+        /* cross-leaf checks that target this leaf: this item's chunk */
+        uint32_t tb, te;
+        item_checks(a, g, chunk, tb, te);
         for (uint32_t t = tb; t < te; ++t) {
             const uint2 qe = a.tlist[t];
             const uint32_t q = qe.x;
@@ -142,6 +145,23 @@ size_t refine_smem_bytes(uint32_t cap) {
     return (size_t)kRefineWarps * ((per_warp + 63) & ~(size_t)63);
 }
 
+/* the chunks beyond the first of every leaf's cross-leaf checks */
+__global__ void __launch_bounds__(256) k_refine_extra(const uint32_t *__restrict__ work,
+                                                      const uint32_t *__restrict__ tstart, uint2 *__restrict__ extra,
+                                                      uint64_t cap, DevCounters *cnt) {
+    const uint32_t nwork = cnt->n_leaf_work;
+    for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < nwork; li += gridDim.x * blockDim.x) {
+        const uint32_t g = work[li];
+        const uint32_t cross = tstart[g + 1] - tstart[g];
+        const uint32_t chunks = (cross + kCrossChunk - 1) / kCrossChunk;
+        for (uint32_t ch = 1; ch < chunks; ++ch) {
+            const uint32_t idx = atomicAdd(&cnt->n_extra, 1u);
+            if (idx < cap) extra[idx] = make_uint2(g, ch);
+            else atomicOr(&cnt->error_flags, GLINT_EF_CHECKS_OVERFLOW);
+        }
+    }
+}
+
 RefineArgs refine_args(glint_ctx *c) {
     RefineArgs a;
     a.work = c->d_leaf_work;
@@ -160,6 +180,7 @@ RefineArgs refine_args(glint_ctx *c) {
     a.rank_of = c->d_rank_of;
     a.qstart = c->d_qstart;
     a.qlist = c->d_qlist;
+    a.extra = c->d_rextra;
     a.tab = c->d_tab;
     a.stamp = c->d_stamp;
     a.newlist = c->d_new;
@@ -176,6 +197,8 @@ cudaError_t launch_refine_precision(glint_ctx *c, const RefineArgs &a);
 
 cudaError_t launch_refine(glint_ctx *c, uint32_t /*cur_time*/) {
     RefineArgs a = refine_args(c);
+    k_refine_extra<<<grid_for(c->G, 256), 256, 0, c->stream>>>(c->d_leaf_work, c->d_tstart, c->d_rextra,
+                                                               c->rextra_cap, c->d_cnt);
     if (c->cfg.precision_mode == 1) return launch_refine_precision(c, a);
     k_refine_fp64<<<152 * 8, 32 * kRefineWarps, refine_smem_bytes(c->cap), c->stream>>>(a);
     return cudaGetLastError();

@@ -36,6 +36,7 @@ struct RefineArgs {
     const uint32_t *rank_of;
     const uint32_t *qstart;
     const uint32_t *qlist;
+    const uint2 *extra;        /* (leaf, chunk) items beyond each leaf's first chunk */
     TRec *tab;
     uint8_t *stamp;
     NewEntry *newlist;
@@ -153,6 +154,52 @@ __device__ inline void enqueue(const RefineArgs &a, QEntry *Q, uint32_t &qn, boo
         __syncwarp();
         qn = rest;
     }
+}
+
+/* Work items: a leaf's inside pairs with its first kCrossChunk cross-leaf
+ * checks, and one item per further chunk of its checks.  Dense leaves are
+ * the target of thousands of checks; split into chunks they spread over the
+ * warps instead of leaving a long tail on one.  Every event carries its
+ * position in the reference's order, so the split does not change results. */
+/* warp-collective: the next item, extra chunks first (the long work first);
+ * false when none is left */
+__device__ inline bool claim_item(const RefineArgs &a, uint32_t nwork, uint32_t n_extra, bool &extra_done,
+                                  uint32_t &g, uint32_t &chunk) {
+    const int lane = threadIdx.x & 31;
+    uint32_t v = 0, kind = 0;
+    if (lane == 0) {
+        if (!extra_done) {
+            v = atomicAdd(&a.cnt->extra_next, 1u);
+            if (v < n_extra) kind = 1;
+        }
+        if (kind == 0) {
+            v = atomicAdd(&a.cnt->work_next, 1u);
+            kind = v < nwork ? 2u : 0u;
+        }
+    }
+    kind = __shfl_sync(0xffffffffu, kind, 0);
+    v = __shfl_sync(0xffffffffu, v, 0);
+    if (kind == 1) {
+        const uint2 e = a.extra[v];
+        g = e.x;
+        chunk = e.y;
+        return true;
+    }
+    extra_done = true;
+    if (kind == 2) {
+        g = a.work[v];
+        chunk = 0;
+        return true;
+    }
+    return false;
+}
+
+/* the cross-leaf checks of one item */
+__device__ inline void item_checks(const RefineArgs &a, uint32_t g, uint32_t chunk, uint32_t &tb, uint32_t &te) {
+    const uint32_t b = a.tstart[g], e = a.tstart[g + 1];
+    tb = b + chunk * kCrossChunk;
+    te = tb + kCrossChunk < e ? tb + kCrossChunk : e;
+    if (tb > e) tb = e;
 }
 
 /* does object obj have a cross-leaf check on grid gid */
