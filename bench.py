@@ -312,7 +312,7 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
 # dram__bytes_write.sum) from the one-pass ncu launch list of the tuned step
 # at 10M objects and 2^30 buckets (profiles/step10m_tuned_dram.md); other
 # workloads report null
-TRAFFIC_10M_2P30 = {"refine": 42.7e9, "identify": 50.3e9, "insert": 26.1e9}
+TRAFFIC_10M_2P30 = {"refine": 43.0e9, "identify": 50.6e9, "insert": 26.5e9}
 
 
 def roofline(form, N, buckets=None, mode=None):

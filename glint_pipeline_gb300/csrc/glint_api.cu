@@ -654,9 +654,10 @@ static void fill_stats(glint_ctx *c, glint_step_stats *st) {
     st->band_pairs = h.band_pairs;
     st->box_band = h.box_band;
     st->error_flags = h.error_flags;
-    /* kernels per step: partition 9, filter 9, refine 1, insert 1,
-     * identify 6 + keys 1, schema update 11, tail 1 (scans count three each) */
-    st->launches = 9 + 9 + 1 + 1 + 7 + (c->cfg.dynamic_schema ? 11 : 0) + 1;
+    /* kernels per step: partition 9, filter 9, refine 2 (work items, pairs),
+     * insert 1, identify 6 + keys 1, schema update 11, tail 1 (scans count
+     * three each) */
+    st->launches = 9 + 9 + 2 + 1 + 7 + (c->cfg.dynamic_schema ? 11 : 0) + 1;
     st->meeting_log_size = h.log_head;
     st->kv_count = h.kv_count;
     st->flushed = c->last_flushed ? 1u : 0u;
