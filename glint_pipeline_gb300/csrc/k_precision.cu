@@ -14,6 +14,8 @@
  */
 #include <cstring>
 
+#include <atomic>
+
 #include "refine_common.cuh"
 
 namespace glint {
@@ -170,9 +172,16 @@ cudaError_t launch_refine_precision(glint_ctx *c, const RefineArgs &a) {
     return cudaGetLastError();
 }
 
+/* as refine_set_attributes: the limit only grows (it is per kernel, not
+ * per context) */
 void refine_prec_set_attributes(uint32_t cap) {
+    static std::atomic<uint32_t> largest{0};
+    uint32_t m = largest.load();
+    while (cap > m && !largest.compare_exchange_weak(m, cap)) {
+    }
+    const uint32_t use = cap > m ? cap : m;
     cudaFuncSetAttribute(k_refine_fp32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)refine_prec_smem_bytes(cap));
+                         (int)refine_prec_smem_bytes(use));
 }
 
 /* ---- probe: the screen against the FP64 test on sampled pairs --------------

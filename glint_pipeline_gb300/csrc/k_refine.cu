@@ -23,6 +23,8 @@
  * id is dropped when the other test also passes, so every pair has at most
  * one event per step.
  */
+#include <atomic>
+
 #include "refine_common.cuh"
 
 namespace glint {
@@ -204,8 +206,16 @@ cudaError_t launch_refine(glint_ctx *c, uint32_t /*cur_time*/) {
     return cudaGetLastError();
 }
 
+/* The limit is a property of the kernel, shared by every context of the
+ * process: it only ever grows, to the largest leaf buffer asked for, so that
+ * creating a context with a small buffer never breaks one with a larger. */
 void refine_set_attributes(uint32_t cap) {
-    cudaFuncSetAttribute(k_refine_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)refine_smem_bytes(cap));
+    static std::atomic<uint32_t> largest{0};
+    uint32_t m = largest.load();
+    while (cap > m && !largest.compare_exchange_weak(m, cap)) {
+    }
+    const uint32_t use = cap > m ? cap : m;
+    cudaFuncSetAttribute(k_refine_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)refine_smem_bytes(use));
 }
 
 /* ---- insertion of the step's new pairs -------------------------------------
