@@ -877,7 +877,8 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
     unsigned int *d_nbig = reinterpret_cast<unsigned int *>(c->d_fmisc + 2);
     cudaMemsetAsync(c->d_fmisc, 0, sizeof(unsigned long long) * 8, s);
     cudaMemsetAsync(c->d_bitmaps, 0, total_bits / 8, s);
-    cudaMemsetAsync(c->d_ctf_keys, 0, c->kv_cap * 16, s);
+    /* d_ctf_keys needs no clearing: the packing writes every byte of the
+     * key_bytes it holds, and nothing reads past them */
 
     /* STR: by mean x (full 64-bit key), then by y inside each x-slice */
     if ((e = radix_sort_u64(c->d_mid, c->d_oids, c->d_mid2, c->d_oids2, N, 64, c->d_rs_tmp, c->d_scan_tmp, s)))
