@@ -144,6 +144,12 @@ def _load_oracle():
     lib.go_sin_cr.argtypes = [ctypes.c_double]
     lib.go_cantor.restype = ctypes.c_uint64
     lib.go_cantor.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+    lib.go_compact.restype = ctypes.c_int
+    lib.go_compact.argtypes = [vp, ctypes.c_uint32, ctypes.c_uint32, vp, ctypes.c_uint32, ctypes.c_uint32,
+                               ctypes.c_int, ctypes.POINTER(vp)]
+    lib.go_compact_sizes.argtypes = [vp, vp]
+    lib.go_compact_result.argtypes = [vp] * 9
+    lib.go_compact_free.argtypes = [vp]
     return lib
 
 
@@ -245,6 +251,64 @@ def query_bfs(edges: np.ndarray, num_objects: int, seeds, hops: int, t_start: in
                      out.ctypes.data, out.shape[0], hop_end.ctypes.data)
     bounds = [0] + [int(v) for v in hop_end[:hops]]
     return [out[bounds[h]:bounds[h + 1]] for h in range(hops)]
+
+
+class GoBlock(ctypes.Structure):
+    """go_block: one source block of a compaction"""
+    _fields_ = [("CTF_count", ctypes.c_uint32), ("o_count", ctypes.c_uint32), ("sids", ctypes.c_void_p),
+                ("ctfs", ctypes.c_void_p), ("keys", ctypes.c_void_p), ("o_keys", ctypes.c_void_p),
+                ("o_boxes", ctypes.c_void_p), ("o_bitmap", ctypes.c_void_p), ("o_times", ctypes.c_uint32 * 4),
+                ("times", ctypes.c_uint32 * 4)]
+
+
+COMPACT_ERRORS = {-1: "no object has a CTF key", -2: "too few objects for split_num",
+                  -3: "an object id beyond num_objects", -4: "get_ctf_bits out of domain"}
+
+
+def compact_blocks(blocks, num_objects, mbr, split_num, max_meet_time=4096, std_ties=False):
+    """CPU restatement of the reference's merge_dump (glint_compact_oracle.c).
+
+    blocks: dicts with keys, sids, ctfs, o_keys, o_boxes, o_bitmap, o_times
+    (4) and times (4), as Store.result / the device store give them.
+    std_ties: equivalent elements in the order of the C++ library's std::sort
+    (the reference's exact output) instead of a stable order (the device's).
+    Returns (rc, result dict or None)."""
+    lib = oracle_lib()
+    keep = []
+    arr = (GoBlock * len(blocks))()
+    for i, b in enumerate(blocks):
+        fields = {}
+        for k in ("sids", "ctfs", "keys", "o_keys", "o_boxes", "o_bitmap"):
+            a = np.ascontiguousarray(b[k])
+            if a.size == 0:
+                a = np.zeros(16, np.uint8)
+            keep.append(a)
+            fields[k] = a.ctypes.data
+        arr[i] = GoBlock(len(b["ctfs"]), len(b["o_keys"]), fields["sids"], fields["ctfs"], fields["keys"],
+                         fields["o_keys"], fields["o_boxes"], fields["o_bitmap"],
+                         (ctypes.c_uint32 * 4)(*[int(v) for v in b["o_times"]]),
+                         (ctypes.c_uint32 * 4)(*[int(v) for v in b.get("times", (0, 0, 0, 0))]))
+    m = np.ascontiguousarray(mbr, dtype=np.float64)
+    h = ctypes.c_void_p()
+    rc = lib.go_compact(ctypes.cast(arr, ctypes.c_void_p), len(blocks), int(num_objects), m.ctypes.data,
+                        int(max_meet_time), int(split_num), int(bool(std_ties)), ctypes.byref(h))
+    if rc != 0:
+        return rc, None
+    try:
+        sizes = np.zeros(8, np.uint64)
+        lib.go_compact_sizes(h, sizes.ctypes.data)
+        C, kv, kb, on = (int(v) for v in sizes[:4])
+        out = {"keys": np.zeros(kb, np.uint8), "sids": np.zeros(int(num_objects), np.uint16),
+               "ctfs": np.zeros(C, CTF_META_DTYPE), "bitmaps": np.zeros(C * BIT_BYTES, np.uint8),
+               "o_keys": np.zeros((on, 16), np.uint8), "o_boxes": np.zeros((on, 4), np.float32),
+               "o_bitmap": np.zeros(BIT_BYTES, np.uint8), "times8": np.zeros(8, np.uint32)}
+        lib.go_compact_result(h, *[out[k].ctypes.data for k in
+                                   ("keys", "sids", "ctfs", "bitmaps", "o_keys", "o_boxes", "o_bitmap", "times8")])
+        out.update(kv_count=kv, key_bytes=kb, o_count=on, padding=int(sizes[4]), x_part=int(sizes[5]),
+                   y_part=int(sizes[6]), sid_count=int(sizes[7]))
+        return 0, out
+    finally:
+        lib.go_compact_free(h)
 
 
 class Store:
@@ -370,6 +434,10 @@ def ref_lib():
         lib.ref_store_find.restype = ctypes.c_uint32
         lib.ref_store_find.argtypes = [vp, ctypes.c_uint32]
         lib.ref_store_free.argtypes = [vp]
+        lib.ref_compact.restype = ctypes.c_int
+        lib.ref_compact.argtypes = [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_uint32,
+                                    ctypes.c_uint32, ctypes.c_uint32, vp, ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.c_char_p]
         _REF = lib
     return _REF
 

@@ -28,7 +28,9 @@ for f in filter refinement meeting workbench step_merge analyze; do
     $CXX $FLAGS -c "$SRC/tracing/$f.cpp" -o "$OUT/$f.o" &
     objs="$objs $OUT/$f.o"
 done
+# the compaction tool, its main() renamed so that merge_dump can be called
+$CXX $FLAGS -Dmain=glint_ref_compaction_tool_main -c "$SRC/tools/compaction.cpp" -o "$OUT/compaction.o" &
 $CXX $FLAGS -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o" &
 wait
-$CXX -shared -o "$OUT/libglintref.so" $objs "$OUT/ref_driver.o" -pthread -fopenmp -lm
+$CXX -shared -o "$OUT/libglintref.so" $objs "$OUT/compaction.o" "$OUT/ref_driver.o" -pthread -fopenmp -lm
 echo "built $OUT/libglintref.so"

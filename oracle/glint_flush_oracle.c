@@ -552,3 +552,14 @@ uint64_t go_store_sorted(const go_store *s, void *keys, float *boxes) {
     if (boxes) memcpy(boxes, s->boxes, sizeof(float) * 4 * n);
     return n;
 }
+
+/* the CTF encoding helpers for the compaction restatement */
+int go_ctf_bits(go_ctf_meta *c, const double *map4, uint32_t num_objects, uint32_t max_meet_time) {
+    go_store_config cfg;
+    memset(&cfg, 0, sizeof(cfg));
+    cfg.num_objects = num_objects;
+    cfg.max_meet_time = max_meet_time;
+    return ctf_bits(c, map4, &cfg);
+}
+
+uint64_t go_serialize_box(const float *box4, const go_ctf_meta *c) { return serialize_box(box4, c); }

@@ -193,6 +193,46 @@ uint64_t go_query_bfs(const go_edge *edges, uint64_t n_edges, uint32_t num_objec
  * check how often libm's sin differs from the correctly rounded value */
 double go_sin_cr(double x);
 
+/* CTF::get_ctf_bits on c->ctf_mbr (fills the bit widths, grids and bitmap
+ * size); 0 where the reference's asserts fire.  serialize_mbr of a box. */
+int go_ctf_bits(go_ctf_meta *c, const double *map4, uint32_t num_objects, uint32_t max_meet_time);
+uint64_t go_serialize_box(const float *box4, const go_ctf_meta *c);
+
+/* ---- compaction of stored blocks (glint_compact_oracle.c;
+ * tools/compaction.cpp:729-1215) ---- */
+/* one source block as the store holds it */
+typedef struct go_block {
+    uint32_t CTF_count, o_count;
+    const uint16_t *sids;          /* num_objects */
+    const go_ctf_meta *ctfs;       /* CTF_count */
+    const uint8_t *keys;           /* the CTFs' packed keys, one CTF after another */
+    const uint8_t *o_keys;         /* o_count 16-byte little-endian keys */
+    const float *o_boxes;          /* o_count x 4 */
+    const uint8_t *o_bitmap;       /* 8192 bytes */
+    uint32_t o_times[4];           /* oversize buffer start_time_min/max, end_time_min/max */
+    uint32_t times[4];             /* the CTB record's start_time_min/max, end_time_min/max */
+} go_block;
+
+typedef struct go_compaction go_compaction;
+/* merges `count` blocks into one of split_num^2 CTFs; 0 on success, < 0
+ * where merge_dump leaves its domain (GO_CMP_* below).  std_ties: order
+ * equivalent elements as the C++ library's std::sort does (the reference's
+ * exact output); 0: keep them in a stable order (the device path's). */
+int go_compact(const go_block *blocks, uint32_t count, uint32_t num_objects, const double *map4,
+               uint32_t max_meet_time, uint32_t split_num, int std_ties, go_compaction **out);
+#define GO_CMP_NO_KEYS (-1)        /* no object has a CTF key */
+#define GO_CMP_PARTITION (-2)      /* too few objects for split_num: a partition size underflows */
+#define GO_CMP_OID (-3)            /* a decoded object id beyond num_objects */
+#define GO_CMP_CTF_BITS (-4)       /* get_ctf_bits asserts (an empty CTF, too many key bits) */
+/* sizes[8]: CTF_count, kv_count, key_bytes, o_count, padding (entries of oid
+ * 0 that fill the per-CTF object lists), x_part, y_part, sid_count (objects
+ * placed in CTFs) */
+void go_compact_sizes(const go_compaction *h, uint64_t *sizes);
+/* times8: the CTB record's start/end times, then the oversize buffer's */
+void go_compact_result(const go_compaction *h, uint8_t *keys, uint16_t *sids, go_ctf_meta *ctfs, uint8_t *bitmaps,
+                       void *o_keys, float *o_boxes, uint8_t *o_bitmap, uint32_t *times8);
+void go_compact_free(go_compaction *h);
+
 #ifdef __cplusplus
 }
 #endif

@@ -384,4 +384,67 @@ void ref_store_free(void *hv) {
     delete h;
 }
 
+/* ---- the reference's compaction (merge_dump, tools/compaction.cpp:729-1215),
+ * built from the tool's own source with its main() renamed ---- */
+int ref_compact(const char *meta_prefix, const char *raid_path, const char *keys_prefix, uint32_t count,
+                uint32_t num_objects, uint32_t CTF_count, const double *map4, uint32_t max_meet_time,
+                uint32_t split_num, const char *out_meta_path);
+
 } /* extern "C" */
+
+void *merge_dump(workbench *bench, uint start_ctb, uint merge_ctb_count, vector<vector<key_info>> &keys_with_sid,
+                 vector<vector<f_box>> &mbrs_with_sid, vector<vector<uint>> &invert_index,
+                 vector<pair<vector<key_info>, vector<f_box>>> &objects_map, vector<object_info> &str_list);
+
+/* serialize_mbr (cuda/geometry.cu:162-172) lives in the GPU sources, which g++
+ * does not build; the compaction tool calls it only with its CTF's own box,
+ * for which CTF::serial_mbr (tracing/step_merge.cpp:290-310) is the same
+ * arithmetic */
+uint64_t serialize_mbr(f_box *b, f_box *bitmap_mbr, CTF *ctf) {
+    (void)bitmap_mbr;
+    return ctf->serial_mbr(b);
+}
+
+/* load_meta (tracing/process.cpp:213-236) is called only by the tool's own
+ * main(), which is never run here */
+workbench *load_meta(const char *, uint, uint) { return nullptr; }
+
+/* blocks 0 .. count-1 read from <meta_prefix>_CTB<i> and their SSTables, as
+ * load_meta does, then merged by merge_dump as the tool's main() calls it;
+ * the result goes to <out_meta_path><2 count>G_CTB0 / _STcL0-<i> and
+ * <raid_path><i % 2>/<2 count>G_SSTable_0-<i> */
+extern "C" int ref_compact(const char *meta_prefix, const char *raid_path, const char *keys_prefix, uint32_t count,
+                           uint32_t num_objects, uint32_t CTF_count, const double *map4, uint32_t max_meet_time,
+                           uint32_t split_num, const char *out_meta_path) {
+    configuration *c = new configuration();
+    c->num_objects = num_objects;
+    c->CTF_count = CTF_count;
+    c->split_num = split_num;
+    c->G_bytes = 2 * count;       /* the output prefix is "<G_bytes>G" */
+    c->max_meet_time = max_meet_time;
+    c->num_threads = 1;
+    std::strncpy(c->raid_path, raid_path, sizeof(c->raid_path) - 1);
+    std::strncpy(c->CTB_meta_path, out_meta_path, sizeof(c->CTB_meta_path) - 1);
+    workbench *b = new workbench(c);
+    b->bit_count = 256 * 256;
+    /* merge_dump ORs bitmaps_size bytes of each source oversize bitmap, which
+     * holds bit_count / 8; only the first bit_count / 8 are written out, so
+     * the read is kept inside the buffers */
+    b->bitmaps_size = b->bit_count / 8;
+    b->mbr = box(map4[0], map4[1], map4[2], map4[3]);
+    std::strncpy(b->keys_file_prefix, keys_prefix, sizeof(b->keys_file_prefix) - 1);
+    b->ctbs = new CTB[count];
+    for (uint32_t i = 0; i < count; ++i) b->load_CTB_meta(meta_prefix, (int)i);
+    const uint new_count = split_num * split_num;
+    vector<object_info> str_list(num_objects);
+    vector<vector<key_info>> keys_with_sid(new_count);
+    vector<vector<f_box>> mbrs_with_sid(new_count);
+    vector<vector<uint>> invert_index(new_count);
+    vector<pair<vector<key_info>, vector<f_box>>> objects_map(num_objects);
+    merge_dump(b, 0, count, keys_with_sid, mbrs_with_sid, invert_index, objects_map, str_list);
+    delete[] b->ctbs;
+    b->ctbs = nullptr;
+    delete b;
+    delete c;
+    return 0;
+}
