@@ -223,15 +223,69 @@ class DeviceBench:
         if st != 0:
             raise GlintError(st, self.last_error())
 
-    def load_store(self, raid_path: str, meta_path: str, prefix: str, ctb: int = 0):
+    def load_store(self, raid_path: str, meta_path: str, prefix: str, ctb: int = 0, ctf_count: int | None = None):
         """One block's files (written here or by the reference) into a kept
-        block for queries (workbench::load_CTB_meta and friends)."""
-        st = self.lib.glint_store_load(self.h, raid_path.encode(), meta_path.encode(), prefix.encode(), int(ctb))
+        block for queries (workbench::load_CTB_meta and friends); ctf_count
+        for a compacted block (its record does not carry it)."""
+        if ctf_count is None:
+            st = self.lib.glint_store_load(self.h, raid_path.encode(), meta_path.encode(), prefix.encode(), int(ctb))
+        else:
+            st = self.lib.glint_store_load_ctfs(self.h, raid_path.encode(), meta_path.encode(), prefix.encode(),
+                                                int(ctb), int(ctf_count))
         if st != 0:
             raise GlintError(st, self.last_error())
 
     def store_blocks(self) -> int:
         return int(self.lib.glint_store_blocks(self.h))
+
+    def block_info(self, block: int) -> "_abi.GlintBlockInfo":
+        info = _abi.GlintBlockInfo()
+        st = self.lib.glint_store_block_info(self.h, int(block), ctypes.byref(info))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        return info
+
+    def block(self, block: int) -> dict:
+        """A kept block (0 = the oldest) as host arrays, in the layout of
+        store(); "times" are the CTB record's, "o_times" the oversize
+        buffer's."""
+        bi = self.block_info(block)
+        info = bi.store
+        C = int(bi.CTF_count)
+        out = {"keys": np.zeros(int(info.key_bytes), np.uint8), "sids": np.zeros(self.n, np.uint16),
+               "ctfs": np.zeros(C, _abi.CTF_META_DTYPE), "bitmaps": np.zeros(C * _abi.BITMAP_BYTES, np.uint8),
+               "o_keys": np.zeros((int(info.oversize_kv_count), 16), np.uint8),
+               "o_boxes": np.zeros((int(info.oversize_kv_count), 4), np.float32),
+               "o_bitmap": np.zeros(_abi.BITMAP_BYTES, np.uint8)}
+        ptr = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        st = self.lib.glint_store_block_read(self.h, int(block), ptr(out["keys"]), ptr(out["sids"]),
+                                             ptr(out["ctfs"]), ptr(out["bitmaps"]), ptr(out["o_keys"]),
+                                             ptr(out["o_boxes"]), ptr(out["o_bitmap"]))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        out["ctf_capacity"] = out["ctfs"]["CTF_kv_capacity"].copy()
+        out["times"] = list(bi.times)
+        out["o_times"] = [info.oversize_start_time_min, info.oversize_start_time_max, info.oversize_end_time_min,
+                          info.oversize_end_time_max]
+        out["info"] = info
+        return out
+
+    def dump_block(self, block: int, raid_path: str, meta_path: str, prefix: str, ctb: int = 0):
+        """A kept block into files in the reference's layout."""
+        st = self.lib.glint_store_block_dump(self.h, int(block), raid_path.encode(), meta_path.encode(),
+                                             prefix.encode(), int(ctb))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+
+    def compact(self, first: int, count: int, split_num: int) -> dict:
+        """Merge kept blocks [first, first + count) into one block of
+        split_num^2 CTFs (merge_dump, tools/compaction.cpp:729-1215), which
+        takes their place among the kept blocks."""
+        info = _abi.GlintCompactInfo()
+        st = self.lib.glint_store_compact(self.h, int(first), int(count), int(split_num), ctypes.byref(info))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        return info.as_dict()
 
     def query(self, queries):
         """Contact-trace queries over the kept store blocks.  queries: a list of

@@ -148,6 +148,22 @@ class GlintStoreView(ctypes.Structure):
                 ("oversize_bitmap", ctypes.c_void_p), ("info", GlintStoreInfo)]
 
 
+class GlintBlockInfo(ctypes.Structure):
+    """glint_block_info: a kept block's CTF count, CTB record times and sizes"""
+    _fields_ = [("CTF_count", ctypes.c_uint32), ("times", ctypes.c_uint32 * 4), ("reserved", ctypes.c_uint32),
+                ("store", GlintStoreInfo)]
+
+
+class GlintCompactInfo(ctypes.Structure):
+    _fields_ = [("CTF_count", ctypes.c_uint32), ("blocks", ctypes.c_uint32), ("kv_count", ctypes.c_uint64),
+                ("key_bytes", ctypes.c_uint64), ("padding", ctypes.c_uint64), ("oversize_kv_count", ctypes.c_uint32),
+                ("sid_count", ctypes.c_uint32), ("x_part", ctypes.c_uint32), ("y_part", ctypes.c_uint32),
+                ("ms", ctypes.c_float), ("reserved", ctypes.c_uint32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
 class GlintQuery(ctypes.Structure):
     _fields_ = [("seeds", ctypes.c_void_p), ("n_seeds", ctypes.c_uint32), ("hops", ctypes.c_uint32),
                 ("t_start", ctypes.c_uint32), ("t_end", ctypes.c_uint32)]
@@ -219,6 +235,11 @@ def load_library(path: str | None = None):
     lib.glint_store_file_error.restype = ctypes.c_char_p
     lib.glint_store_dump.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
     lib.glint_store_load.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
+    lib.glint_store_load_ctfs.argtypes = [vp, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32, u32]
+    lib.glint_store_block_info.argtypes = [vp, u32, ctypes.POINTER(GlintBlockInfo)]
+    lib.glint_store_block_read.argtypes = [vp, u32] + [vp] * 7
+    lib.glint_store_block_dump.argtypes = [vp, u32, ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p, u32]
+    lib.glint_store_compact.argtypes = [vp, u32, u32, u32, ctypes.POINTER(GlintCompactInfo)]
     lib.glint_snapshot_save.argtypes = [vp, ctypes.c_char_p]
     lib.glint_snapshot_load.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(vp)]
     lib.glint_trace_open.argtypes = [ctypes.c_char_p, u32, u32, u32, u32, ctypes.POINTER(vp)]

@@ -27,7 +27,7 @@ TRACEGEN = os.path.join(HERE, "_tracegen.so")
 CU_SOURCES = ["glint_api.cu", "k_util.cu", "k_partition.cu", "k_filter.cu", "k_refine.cu", "k_identify.cu",
               "k_schema.cu", "k_precision.cu", "k_flush.cu", "k_query.cu", "k_sort.cu",
               "k_serve.cu", "glint_batch.cu", "store_files.cu",
-              "glint_pipe.cu", "trace_files.cu", "snapshot.cu"]
+              "glint_pipe.cu", "trace_files.cu", "snapshot.cu", "k_compact.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

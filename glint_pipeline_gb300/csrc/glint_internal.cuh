@@ -92,7 +92,8 @@ struct SchemaEvent {
     uint32_t kind;        /* 0 split, 1 merge */
 };
 
-/* one flushed contact-tracing block (CTB) kept on the device for queries */
+/* one contact-tracing block (CTB) kept on the device: flushed, loaded from
+ * files or compacted */
 struct StoreBlock {
     uint8_t *keys = nullptr;               /* packed CTF keys */
     uint64_t key_bytes = 0;
@@ -101,9 +102,17 @@ struct StoreBlock {
     uint16_t *sids = nullptr;              /* [N] 0 none, 1 oversize, 2.. CTF + 2 */
     uint32_t *first = nullptr, *count = nullptr; /* [N] each object's keys (in its CTF or the oversize buffer) */
     ulonglong2 *okeys = nullptr;           /* oversize keys, 128-bit */
+    float4 *oboxes = nullptr;              /* [o_count] oversize boxes */
+    uint8_t *bitmaps = nullptr;            /* [C][8192] CTF bitmaps */
+    uint8_t *obitmap = nullptr;            /* [8192] oversize bitmap */
     uint64_t kv = 0, o_count = 0;
-    uint32_t end_time_min = 0, end_time_max = 0;
+    uint32_t end_time_min = 0, end_time_max = 0; /* base of the key end offsets; last step */
+    uint32_t C = 0;                        /* CTFs */
+    uint32_t o_times[4] = {0, 0, 0, 0};    /* oversize buffer start_time_min/max, end_time_min/max */
+    uint32_t rec_times[4] = {0, 0, 0, 0};  /* the CTB record's own start/end time fields */
+    uint32_t sid_count = 0, oversize_oid_count = 0;
 };
+void store_block_release(StoreBlock &b);
 
 /* device-side descriptor of a StoreBlock */
 struct StoreBlockDev {
@@ -271,6 +280,13 @@ void flush_free(glint_ctx *c);
 void flush_set_attributes();
 glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err);
 void store_blocks_free(glint_ctx *c);
+/* CTF::get_ctf_bits + eight_parallel on the host (k_flush.cu) */
+bool ctf_bits(glint_ctf_meta &c, const glint_box &map, uint32_t num_objects, uint32_t max_meet_time);
+/* stable LSD radix sort of (u64 key, u32 value) pairs (k_sort.cu) */
+cudaError_t radix_sort_u64(unsigned long long *keys, uint32_t *vals, unsigned long long *tmp_k, uint32_t *tmp_v,
+                           uint64_t n, int bits, void *rs_tmp, void *scan_tmp, cudaStream_t s);
+size_t radix_tmp_bytes(uint64_t n);
+int radix_bits_for(unsigned long long max_key);
 void server_free_default(glint_ctx *c);
 void servers_detach(glint_ctx *c);
 

@@ -41,12 +41,10 @@
 #include <vector>
 
 #include "glint_internal.cuh"
+#include "store_codec.cuh"
 
 namespace glint {
 
-cudaError_t radix_sort_u64(unsigned long long *keys, uint32_t *vals, unsigned long long *tmp_k, uint32_t *tmp_v,
-                           uint64_t n, int bits, void *rs_tmp, void *scan_tmp, cudaStream_t s);
-size_t radix_tmp_bytes(uint64_t n);
 
 constexpr int kOidBit = 26;            /* util/util.h:49 */
 constexpr int kSidShift = 2 * kOidBit + 64;
@@ -659,20 +657,6 @@ __global__ void k_ctf_bitmap(const u128 *__restrict__ keys, const float4 *__rest
     }
 }
 
-/* serialize_mbr for f_box (:162-174) */
-__device__ inline uint64_t serialize_box(const float4 &b, const glint_ctf_meta &m) {
-    const float ex = __fsub_rn(m.ctf_mbr[2], m.ctf_mbr[0]), ey = __fsub_rn(m.ctf_mbr[3], m.ctf_mbr[1]);
-    const float longer_edge = fmaxf(ex, ey);
-    const float fx = __ull2float_rn((1ull << m.low_x_bit) - 1), fy = __ull2float_rn((1ull << m.low_y_bit) - 1);
-    const float fe = __ull2float_rn((1ull << m.edge_bit) - 1);
-    const uint64_t low0 = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.x, m.ctf_mbr[0]), ex), fx));
-    const uint64_t low1 = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.y, m.ctf_mbr[1]), ey), fy));
-    const uint64_t x = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.z, b.x), longer_edge), fe));
-    const uint64_t y = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.w, b.y), longer_edge), fe));
-    return (low0 << (m.low_y_bit + m.edge_bit + m.edge_bit)) + (low1 << (m.edge_bit + m.edge_bit)) +
-           (x << m.edge_bit) + y;
-}
-
 /* write_key_and_mbr (:1079-1104), one thread per key */
 __global__ void k_ctf_pack(const u128 *__restrict__ keys, const float4 *__restrict__ boxes, uint64_t kv, CtfTables t,
                            uint8_t *__restrict__ out, uint64_t out_bytes) {
@@ -1032,10 +1016,11 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
         A((void **)&b.first, sizeof(uint32_t) * N);
         A((void **)&b.count, sizeof(uint32_t) * N);
         A((void **)&b.okeys, sizeof(ulonglong2) * o_n);
+        A((void **)&b.oboxes, sizeof(float4) * o_n);
+        A((void **)&b.bitmaps, (size_t)C * kBitCount / 8);
+        A((void **)&b.obitmap, kBitCount / 8);
         if (ae != cudaSuccess) {
-            void *ps[] = {b.keys, b.ctfs, b.key_index, b.byte_index, b.sids, b.first, b.count, b.okeys};
-            for (void *p : ps)
-                if (p) cudaFree(p);
+            store_block_release(b);
             return fail(ae, "keep block");
         }
         if (bytes) cudaMemcpyAsync(b.keys, c->d_ctf_keys, bytes, cudaMemcpyDeviceToDevice, s);
@@ -1043,21 +1028,29 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
         cudaMemcpyAsync(b.key_index, c->d_ctf_lo, sizeof(unsigned long long) * C, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(b.byte_index, c->d_ctf_byte, sizeof(unsigned long long) * C, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(b.sids, c->d_sids, sizeof(uint16_t) * N, cudaMemcpyDeviceToDevice, s);
-        if (o_n)
+        if (o_n) {
             cudaMemcpyAsync(b.okeys, c->d_keys + kv, sizeof(ulonglong2) * o_n, cudaMemcpyDeviceToDevice, s);
+            cudaMemcpyAsync(b.oboxes, c->d_kvbox + kv, sizeof(float4) * o_n, cudaMemcpyDeviceToDevice, s);
+        }
+        cudaMemcpyAsync(b.bitmaps, c->d_bitmaps, (size_t)C * kBitCount / 8, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(b.obitmap, c->d_obitmap, kBitCount / 8, cudaMemcpyDeviceToDevice, s);
         k_block_index<<<grid_for(N, 256), 256, 0, s>>>(N, c->d_segof, c->d_same, c->d_over, kv, b.first, b.count);
         b.kv = kv;
         b.o_count = o_n;
         b.key_bytes = bytes;
         b.end_time_min = c->end_time_min;
         b.end_time_max = c->last_time;
+        b.C = C;
+        b.o_times[0] = inf.oversize_start_time_min;
+        b.o_times[1] = inf.oversize_start_time_max;
+        b.o_times[2] = inf.oversize_end_time_min;
+        b.o_times[3] = inf.oversize_end_time_max;
+        b.sid_count = inf.sid_count;
+        b.oversize_oid_count = inf.oversize_oid_count;
         c->ctbs.push_back(b);
         while (c->ctbs.size() > c->cfg.store_keep) {
-            StoreBlock &o = c->ctbs.front();
             cudaStreamSynchronize(s);
-            void *ps[] = {o.keys, o.ctfs, o.key_index, o.byte_index, o.sids, o.first, o.count, o.okeys};
-            for (void *p : ps)
-                if (p) cudaFree(p);
+            store_block_release(c->ctbs.front());
             c->ctbs.erase(c->ctbs.begin());
         }
     }
@@ -1138,12 +1131,16 @@ extern "C" glint_status glint_store_read(glint_ctx *c, uint8_t *keys, uint16_t *
 }
 
 namespace glint {
+void store_block_release(StoreBlock &b) {
+    void *ps[] = {b.keys,  b.ctfs,  b.key_index, b.byte_index, b.sids,   b.first,
+                  b.count, b.okeys, b.oboxes,    b.bitmaps,    b.obitmap};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    b = StoreBlock();
+}
+
 void store_blocks_free(glint_ctx *c) {
-    for (StoreBlock &o : c->ctbs) {
-        void *ps[] = {o.keys, o.ctfs, o.key_index, o.byte_index, o.sids, o.first, o.count, o.okeys};
-        for (void *p : ps)
-            if (p) cudaFree(p);
-    }
+    for (StoreBlock &o : c->ctbs) store_block_release(o);
     c->ctbs.clear();
 }
 } // namespace glint

@@ -301,7 +301,7 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
     for (uint32_t i = 0; i < nb; ++i) {
         const StoreBlock &b = c->ctbs[i];
         bd[i] = StoreBlockDev{b.keys, b.ctfs, b.key_index, b.byte_index, b.sids, b.first, b.count, b.okeys,
-                              b.end_time_min, c->cfg.CTF_count};
+                              b.end_time_min, b.C};
     }
     if (nb) cudaMemcpyAsync(v->blocks, bd.data(), sizeof(StoreBlockDev) * nb, cudaMemcpyHostToDevice, s);
     HopArgs a = server_args(v, nb);

@@ -28,6 +28,16 @@ namespace {
 
 constexpr uint64_t kMagic = 0x31504E5354494C47ull; /* "GLITSNP1" */
 constexpr uint64_t kTableChunk = 1ull << 22;        /* buckets per transfer */
+constexpr uint32_t kVersion = 2;                    /* 2: kept blocks carry bitmaps, oversize boxes, times */
+constexpr size_t kBitBytes = 65536 / 8;
+
+/* a kept block's scalar fields */
+struct SnapBlock {
+    uint64_t kv, o_count, key_bytes;
+    uint32_t end_time_min, end_time_max, C, sid_count;
+    uint32_t o_times[4], rec_times[4];
+    uint32_t oversize_oid_count, reserved;
+};
 
 struct SnapHeader {
     uint64_t magic;
@@ -136,7 +146,7 @@ extern "C" glint_status glint_snapshot_save(glint_ctx *c, const char *path) {
     SnapHeader h;
     std::memset(&h, 0, sizeof(h));
     h.magic = kMagic;
-    h.version = 1;
+    h.version = kVersion;
     h.header_bytes = sizeof(SnapHeader);
     h.cfg = c->cfg;
     h.mbr = c->mbr;
@@ -226,17 +236,32 @@ extern "C" glint_status glint_snapshot_save(glint_ctx *c, const char *path) {
     }
     /* the blocks kept for queries */
     for (const StoreBlock &b : c->ctbs) {
-        const uint64_t meta[6] = {b.kv, b.o_count, b.key_bytes, b.end_time_min, b.end_time_max, 0};
+        SnapBlock meta;
+        std::memset(&meta, 0, sizeof(meta));
+        meta.kv = b.kv;
+        meta.o_count = b.o_count;
+        meta.key_bytes = b.key_bytes;
+        meta.end_time_min = b.end_time_min;
+        meta.end_time_max = b.end_time_max;
+        meta.C = b.C;
+        meta.sid_count = b.sid_count;
+        meta.oversize_oid_count = b.oversize_oid_count;
+        std::memcpy(meta.o_times, b.o_times, sizeof(meta.o_times));
+        std::memcpy(meta.rec_times, b.rec_times, sizeof(meta.rec_times));
+        const uint32_t BC = b.C;
         w.section(kSecBlock, sizeof(meta));
-        w.raw(meta, sizeof(meta));
+        w.raw(&meta, sizeof(meta));
         if (e == cudaSuccess) e = w.dev(kSecCtfKeys, b.keys, b.key_bytes);
-        if (e == cudaSuccess) e = w.dev(kSecCtfs, b.ctfs, sizeof(glint_ctf_meta) * C);
-        if (e == cudaSuccess) e = w.dev(kSecCtfCap, b.key_index, sizeof(unsigned long long) * C);
-        if (e == cudaSuccess) e = w.dev(kSecCtfCap, b.byte_index, sizeof(unsigned long long) * C);
+        if (e == cudaSuccess) e = w.dev(kSecCtfs, b.ctfs, sizeof(glint_ctf_meta) * BC);
+        if (e == cudaSuccess) e = w.dev(kSecCtfCap, b.key_index, sizeof(unsigned long long) * BC);
+        if (e == cudaSuccess) e = w.dev(kSecCtfCap, b.byte_index, sizeof(unsigned long long) * BC);
         if (e == cudaSuccess) e = w.dev(kSecSidsOut, b.sids, sizeof(uint16_t) * N);
         if (e == cudaSuccess) e = w.dev(kSecSame, b.first, sizeof(uint32_t) * N);
         if (e == cudaSuccess) e = w.dev(kSecSame, b.count, sizeof(uint32_t) * N);
         if (e == cudaSuccess) e = w.dev(kSecStoreKeys, b.okeys, sizeof(ulonglong2) * b.o_count);
+        if (e == cudaSuccess) e = w.dev(kSecStoreBoxes, b.oboxes, sizeof(float4) * b.o_count);
+        if (e == cudaSuccess) e = w.dev(kSecBitmaps, b.bitmaps, (size_t)BC * kBitBytes);
+        if (e == cudaSuccess) e = w.dev(kSecObitmap, b.obitmap, kBitBytes);
     }
     const bool wrote = w.ok;
     if (fclose(w.f) != 0 || !wrote) {
@@ -255,7 +280,7 @@ extern "C" glint_status glint_snapshot_load(const char *path, int device, glint_
     if (!r.f) return GLINT_ERR_INVALID_ARGUMENT;
     SnapHeader h;
     r.raw(&h, sizeof(h));
-    if (!r.ok || h.magic != kMagic || h.version != 1 || h.header_bytes != sizeof(SnapHeader)) {
+    if (!r.ok || h.magic != kMagic || h.version != kVersion || h.header_bytes != sizeof(SnapHeader)) {
         fclose(r.f);
         return GLINT_ERR_INVALID_ARGUMENT;
     }
@@ -368,23 +393,37 @@ extern "C" glint_status glint_snapshot_load(const char *path, int device, glint_
     }
     /* the kept blocks */
     for (uint32_t k = 0; k < h.num_blocks && e == cudaSuccess && r.ok; ++k) {
-        uint64_t mb = 0, meta[6] = {0, 0, 0, 0, 0, 0};
+        uint64_t mb = 0;
+        SnapBlock meta;
         if (!r.section(kSecBlock, mb) || mb != sizeof(meta)) break;
-        r.raw(meta, sizeof(meta));
+        r.raw(&meta, sizeof(meta));
         StoreBlock b;
-        b.kv = meta[0];
-        b.o_count = meta[1];
-        b.key_bytes = meta[2];
-        b.end_time_min = (uint32_t)meta[3];
-        b.end_time_max = (uint32_t)meta[4];
+        b.kv = meta.kv;
+        b.o_count = meta.o_count;
+        b.key_bytes = meta.key_bytes;
+        b.end_time_min = meta.end_time_min;
+        b.end_time_max = meta.end_time_max;
+        b.C = meta.C;
+        b.sid_count = meta.sid_count;
+        b.oversize_oid_count = meta.oversize_oid_count;
+        std::memcpy(b.o_times, meta.o_times, sizeof(b.o_times));
+        std::memcpy(b.rec_times, meta.rec_times, sizeof(b.rec_times));
+        const uint32_t BC = b.C;
         e = r.dev_alloc(kSecCtfKeys, (void **)&b.keys, b.key_bytes);
-        if (e == cudaSuccess && r.ok) e = r.dev_alloc(kSecCtfs, (void **)&b.ctfs, sizeof(glint_ctf_meta) * C);
-        if (e == cudaSuccess && r.ok) e = r.dev_alloc(kSecCtfCap, (void **)&b.key_index, sizeof(unsigned long long) * C);
-        if (e == cudaSuccess && r.ok) e = r.dev_alloc(kSecCtfCap, (void **)&b.byte_index, sizeof(unsigned long long) * C);
+        if (e == cudaSuccess && r.ok) e = r.dev_alloc(kSecCtfs, (void **)&b.ctfs, sizeof(glint_ctf_meta) * BC);
+        if (e == cudaSuccess && r.ok)
+            e = r.dev_alloc(kSecCtfCap, (void **)&b.key_index, sizeof(unsigned long long) * BC);
+        if (e == cudaSuccess && r.ok)
+            e = r.dev_alloc(kSecCtfCap, (void **)&b.byte_index, sizeof(unsigned long long) * BC);
         if (e == cudaSuccess && r.ok) e = r.dev_alloc(kSecSidsOut, (void **)&b.sids, sizeof(uint16_t) * N);
         if (e == cudaSuccess && r.ok) e = r.dev_alloc(kSecSame, (void **)&b.first, sizeof(uint32_t) * N);
         if (e == cudaSuccess && r.ok) e = r.dev_alloc(kSecSame, (void **)&b.count, sizeof(uint32_t) * N);
-        if (e == cudaSuccess && r.ok) e = r.dev_alloc(kSecStoreKeys, (void **)&b.okeys, sizeof(ulonglong2) * b.o_count);
+        if (e == cudaSuccess && r.ok)
+            e = r.dev_alloc(kSecStoreKeys, (void **)&b.okeys, sizeof(ulonglong2) * b.o_count);
+        if (e == cudaSuccess && r.ok)
+            e = r.dev_alloc(kSecStoreBoxes, (void **)&b.oboxes, sizeof(float4) * b.o_count);
+        if (e == cudaSuccess && r.ok) e = r.dev_alloc(kSecBitmaps, (void **)&b.bitmaps, (size_t)BC * kBitBytes);
+        if (e == cudaSuccess && r.ok) e = r.dev_alloc(kSecObitmap, (void **)&b.obitmap, kBitBytes);
         c->ctbs.push_back(b); /* freed with the context, complete or not */
     }
     const bool read_ok = r.ok;

@@ -1,0 +1,31 @@
+/*
+ * store_codec.cuh -- the store's box quantisation, shared by the flush and
+ * the compaction of kept blocks.
+ */
+#ifndef GLINT_STORE_CODEC_CUH_
+#define GLINT_STORE_CODEC_CUH_
+
+#include <cstdint>
+
+#include "glint.h"
+
+namespace glint {
+
+/* serialize_mbr for f_box (cuda/geometry.cu:162-174): float arithmetic,
+ * truncated to integers */
+__device__ inline uint64_t serialize_box(const float4 &b, const glint_ctf_meta &m) {
+    const float ex = __fsub_rn(m.ctf_mbr[2], m.ctf_mbr[0]), ey = __fsub_rn(m.ctf_mbr[3], m.ctf_mbr[1]);
+    const float longer_edge = fmaxf(ex, ey);
+    const float fx = __ull2float_rn((1ull << m.low_x_bit) - 1), fy = __ull2float_rn((1ull << m.low_y_bit) - 1);
+    const float fe = __ull2float_rn((1ull << m.edge_bit) - 1);
+    const uint64_t low0 = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.x, m.ctf_mbr[0]), ex), fx));
+    const uint64_t low1 = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.y, m.ctf_mbr[1]), ey), fy));
+    const uint64_t x = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.z, b.x), longer_edge), fe));
+    const uint64_t y = __float2ull_rz(__fmul_rn(__fdiv_rn(__fsub_rn(b.w, b.y), longer_edge), fe));
+    return (low0 << (m.low_y_bit + m.edge_bit + m.edge_bit)) + (low1 << (m.edge_bit + m.edge_bit)) +
+           (x << m.edge_bit) + y;
+}
+
+} // namespace glint
+
+#endif

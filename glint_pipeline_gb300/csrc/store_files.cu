@@ -17,7 +17,10 @@
  * layouts (CTF 80 bytes, oversize_buffer 48, CTB 128) are restated here.  The
  * reference writes its heap addresses into the pointer fields and its loader
  * overwrites them; here they are written as zero.  straight_dump leaves the
- * CTB's own count and time fields zero, and so does this writer.
+ * CTB's own count and time fields zero, and so does this writer for a
+ * flushed block; a compacted block carries the time fields merge_dump
+ * folds (tools/compaction.cpp:966-976) and a CTF count of zero, as
+ * merge_dump leaves it.
  */
 #include <cstdio>
 #include <cstring>
@@ -106,7 +109,8 @@ bool write_file(const std::string &path, const std::vector<std::pair<const void 
 
 bool read_exact(FILE *f, void *dst, size_t n) { return n == 0 || fread(dst, 1, n, f) == n; }
 
-glint_status write_store(const glint_store_view &v, const Paths &p, std::string &err) {
+glint_status write_store(const glint_store_view &v, const Paths &p, std::string &err,
+                         const uint32_t *rec_times = nullptr) {
     const uint32_t C = v.CTF_count, N = v.num_objects;
     /* SSTables: CTF after CTF in the packed key buffer */
     uint64_t at = 0;
@@ -122,6 +126,12 @@ glint_status write_store(const glint_store_view &v, const Paths &p, std::string 
     /* CTB record, sids, oversize keys, boxes, bitmap */
     FileCTB ctb;
     std::memset(&ctb, 0, sizeof(ctb));
+    if (rec_times) {
+        ctb.start_time_min = rec_times[0];
+        ctb.start_time_max = rec_times[1];
+        ctb.end_time_min = rec_times[2];
+        ctb.end_time_max = rec_times[3];
+    }
     const uint32_t on = v.info.oversize_kv_count;
     ctb.o_buffer.oversize_kv_count = on;
     ctb.o_buffer.start_time_min = v.info.oversize_start_time_min;
@@ -177,13 +187,15 @@ struct HostBlock {
     std::vector<uint16_t> sids;
     std::vector<uint32_t> first, count;
     std::vector<ulonglong2> okeys;
+    std::vector<float4> oboxes;
+    std::vector<uint8_t> bitmaps, obitmap;
     uint64_t kv = 0;
     uint32_t end_time_min = 0, end_time_max = 0;
+    uint32_t o_times[4] = {0, 0, 0, 0}, rec_times[4] = {0, 0, 0, 0};
 };
 
 glint_status read_store(const Paths &p, uint32_t N, uint32_t C, HostBlock &h, std::string &err) {
-    /* CTB record, sids, oversize keys (boxes and bitmap follow; queries do
-     * not use them) */
+    /* CTB record, sids, oversize keys, boxes and bitmap */
     {
         File in;
         in.f = fopen(p.ctb_meta().c_str(), "rb");
@@ -198,17 +210,30 @@ glint_status read_store(const Paths &p, uint32_t N, uint32_t C, HostBlock &h, st
             return GLINT_ERR_INVALID_ARGUMENT;
         }
         h.okeys.resize(ctb.o_buffer.oversize_kv_count);
-        if (!read_exact(in.f, h.okeys.data(), 16 * h.okeys.size())) {
+        h.oboxes.resize(ctb.o_buffer.oversize_kv_count);
+        h.obitmap.resize(kBitmapBytes);
+        if (!read_exact(in.f, h.okeys.data(), 16 * h.okeys.size()) ||
+            !read_exact(in.f, h.oboxes.data(), sizeof(float4) * h.oboxes.size()) ||
+            !read_exact(in.f, h.obitmap.data(), kBitmapBytes)) {
             err = "short CTB file " + p.ctb_meta();
             return GLINT_ERR_INVALID_ARGUMENT;
         }
         h.end_time_min = ctb.o_buffer.end_time_min;
         h.end_time_max = ctb.o_buffer.end_time_max;
+        h.o_times[0] = ctb.o_buffer.start_time_min;
+        h.o_times[1] = ctb.o_buffer.start_time_max;
+        h.o_times[2] = ctb.o_buffer.end_time_min;
+        h.o_times[3] = ctb.o_buffer.end_time_max;
+        h.rec_times[0] = ctb.start_time_min;
+        h.rec_times[1] = ctb.start_time_max;
+        h.rec_times[2] = ctb.end_time_min;
+        h.rec_times[3] = ctb.end_time_max;
     }
-    /* CTF records (the bitmap that follows is not needed for queries) */
+    /* CTF records and their bitmaps */
     h.ctfs.resize(C);
     h.key_index.resize(C);
     h.byte_index.resize(C);
+    h.bitmaps.assign((size_t)C * kBitmapBytes, 0);
     uint64_t kv = 0, bytes = 0;
     for (uint32_t i = 0; i < C; ++i) {
         File in;
@@ -237,8 +262,13 @@ glint_status read_store(const Paths &p, uint32_t N, uint32_t C, HostBlock &h, st
         m.mbr_bit = r.mbr_bit;
         m.x_grid = r.x_grid;
         m.y_grid = r.y_grid;
-        if (m.key_bit == 0 || m.key_bit % 8 || m.key_bit > 128 || m.id_bit == 0 || m.id_bit > 32) {
+        if (m.key_bit == 0 || m.key_bit % 8 || m.key_bit > 128 || m.id_bit == 0 || m.id_bit > 32 ||
+            m.ctf_bitmap_size > kBitmapBytes) {
             err = "CTF record out of range in " + p.ctf_meta(i);
+            return GLINT_ERR_INVALID_ARGUMENT;
+        }
+        if (!read_exact(in.f, h.bitmaps.data() + (size_t)i * kBitmapBytes, m.ctf_bitmap_size)) {
+            err = "short CTF file " + p.ctf_meta(i);
             return GLINT_ERR_INVALID_ARGUMENT;
         }
         h.key_index[i] = kv;
@@ -347,14 +377,26 @@ extern "C" glint_status glint_store_dump(glint_ctx *c, const char *raid_path, co
     return st;
 }
 
-extern "C" glint_status glint_store_load(glint_ctx *c, const char *raid_path, const char *meta_path,
-                                         const char *prefix, uint32_t ctb) {
-    if (!c || !raid_path || !meta_path || !prefix) return GLINT_ERR_INVALID_ARGUMENT;
+/* a block into the context's kept blocks (the oldest dropped beyond
+ * store_keep) */
+static glint_status keep_block(glint_ctx *c, StoreBlock &b) {
+    c->ctbs.push_back(b);
+    while (c->ctbs.size() > c->cfg.store_keep) {
+        cudaStreamSynchronize(c->stream);
+        store_block_release(c->ctbs.front());
+        c->ctbs.erase(c->ctbs.begin());
+    }
+    return GLINT_OK;
+}
+
+extern "C" glint_status glint_store_load_ctfs(glint_ctx *c, const char *raid_path, const char *meta_path,
+                                              const char *prefix, uint32_t ctb, uint32_t ctf_count) {
+    if (!c || !raid_path || !meta_path || !prefix || ctf_count == 0) return GLINT_ERR_INVALID_ARGUMENT;
     if (c->cfg.store_keep == 0) {
         c->last_error = "store load: the context keeps no blocks (store_keep = 0)";
         return GLINT_ERR_STATE;
     }
-    const uint32_t C = c->cfg.CTF_count, N = c->N;
+    const uint32_t C = ctf_count, N = c->N;
     HostBlock h;
     std::string err;
     glint_status st = read_store(Paths{raid_path, meta_path, prefix, ctb}, N, C, h, err);
@@ -379,6 +421,9 @@ extern "C" glint_status glint_store_load(glint_ctx *c, const char *raid_path, co
     A((void **)&b.first, sizeof(uint32_t) * N);
     A((void **)&b.count, sizeof(uint32_t) * N);
     A((void **)&b.okeys, sizeof(ulonglong2) * h.okeys.size());
+    A((void **)&b.oboxes, sizeof(float4) * h.oboxes.size());
+    A((void **)&b.bitmaps, h.bitmaps.size());
+    A((void **)&b.obitmap, h.obitmap.size());
     auto up = [&](void *dst, const void *src, size_t n) {
         if (e == cudaSuccess && n) e = cudaMemcpy(dst, src, n, cudaMemcpyHostToDevice);
     };
@@ -390,10 +435,11 @@ extern "C" glint_status glint_store_load(glint_ctx *c, const char *raid_path, co
     up(b.first, h.first.data(), sizeof(uint32_t) * N);
     up(b.count, h.count.data(), sizeof(uint32_t) * N);
     up(b.okeys, h.okeys.data(), sizeof(ulonglong2) * h.okeys.size());
+    up(b.oboxes, h.oboxes.data(), sizeof(float4) * h.oboxes.size());
+    up(b.bitmaps, h.bitmaps.data(), h.bitmaps.size());
+    up(b.obitmap, h.obitmap.data(), h.obitmap.size());
     if (e != cudaSuccess) {
-        void *ps[] = {b.keys, b.ctfs, b.key_index, b.byte_index, b.sids, b.first, b.count, b.okeys};
-        for (void *p : ps)
-            if (p) cudaFree(p);
+        store_block_release(b);
         c->last_error = std::string("store load: ") + cudaGetErrorString(e);
         return e == cudaErrorMemoryAllocation ? GLINT_ERR_OUT_OF_MEMORY : GLINT_ERR_CUDA;
     }
@@ -402,13 +448,105 @@ extern "C" glint_status glint_store_load(glint_ctx *c, const char *raid_path, co
     b.key_bytes = h.keys.size();
     b.end_time_min = h.end_time_min;
     b.end_time_max = h.end_time_max;
-    c->ctbs.push_back(b);
-    while (c->ctbs.size() > c->cfg.store_keep) {
-        StoreBlock &o = c->ctbs.front();
-        void *ps[] = {o.keys, o.ctfs, o.key_index, o.byte_index, o.sids, o.first, o.count, o.okeys};
-        for (void *p : ps)
-            if (p) cudaFree(p);
-        c->ctbs.erase(c->ctbs.begin());
+    b.C = C;
+    std::memcpy(b.o_times, h.o_times, sizeof(b.o_times));
+    std::memcpy(b.rec_times, h.rec_times, sizeof(b.rec_times));
+    for (uint32_t o = 0; o < N; ++o) {
+        b.sid_count += h.sids[o] >= 2;
+        b.oversize_oid_count += h.sids[o] == 1;
+    }
+    return keep_block(c, b);
+}
+
+extern "C" glint_status glint_store_load(glint_ctx *c, const char *raid_path, const char *meta_path,
+                                         const char *prefix, uint32_t ctb) {
+    if (!c) return GLINT_ERR_INVALID_ARGUMENT;
+    return glint_store_load_ctfs(c, raid_path, meta_path, prefix, ctb, c->cfg.CTF_count);
+}
+
+extern "C" glint_status glint_store_block_info(glint_ctx *c, uint32_t block, glint_block_info *info) {
+    if (!c || !info) return GLINT_ERR_INVALID_ARGUMENT;
+    if (block >= c->ctbs.size()) {
+        c->last_error = "block info: no such kept block";
+        return GLINT_ERR_INVALID_ARGUMENT;
+    }
+    const StoreBlock &b = c->ctbs[block];
+    std::memset(info, 0, sizeof(*info));
+    info->CTF_count = b.C;
+    std::memcpy(info->times, b.rec_times, sizeof(info->times));
+    glint_store_info &st = info->store;
+    st.kv_count = b.kv;
+    st.key_bytes = b.key_bytes;
+    st.oversize_kv_count = (uint32_t)b.o_count;
+    st.oversize_start_time_min = b.o_times[0];
+    st.oversize_start_time_max = b.o_times[1];
+    st.oversize_end_time_min = b.o_times[2];
+    st.oversize_end_time_max = b.o_times[3];
+    st.sid_count = b.sid_count;
+    st.oversize_oid_count = b.oversize_oid_count;
+    st.end_time_min = b.end_time_min;
+    st.cur_time = b.end_time_max;
+    return GLINT_OK;
+}
+
+extern "C" glint_status glint_store_block_read(glint_ctx *c, uint32_t block, uint8_t *keys, uint16_t *sids,
+                                               glint_ctf_meta *ctfs, uint8_t *bitmaps, void *oversize_keys,
+                                               float *oversize_boxes, uint8_t *oversize_bitmap) {
+    if (!c) return GLINT_ERR_INVALID_ARGUMENT;
+    if (block >= c->ctbs.size()) {
+        c->last_error = "block read: no such kept block";
+        return GLINT_ERR_INVALID_ARGUMENT;
+    }
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    const StoreBlock &b = c->ctbs[block];
+    auto down = [&](void *dst, const void *src, size_t n) {
+        if (e == cudaSuccess && dst && n) e = cudaMemcpy(dst, src, n, cudaMemcpyDeviceToHost);
+    };
+    down(keys, b.keys, b.key_bytes);
+    down(sids, b.sids, sizeof(uint16_t) * (size_t)c->N);
+    down(ctfs, b.ctfs, sizeof(glint_ctf_meta) * b.C);
+    down(bitmaps, b.bitmaps, (size_t)b.C * kBitmapBytes);
+    down(oversize_keys, b.okeys, sizeof(ulonglong2) * b.o_count);
+    down(oversize_boxes, b.oboxes, sizeof(float4) * b.o_count);
+    down(oversize_bitmap, b.obitmap, kBitmapBytes);
+    if (e != cudaSuccess) {
+        c->last_error = std::string("block read: ") + cudaGetErrorString(e);
+        return GLINT_ERR_CUDA;
     }
     return GLINT_OK;
+}
+
+extern "C" glint_status glint_store_block_dump(glint_ctx *c, uint32_t block, const char *raid_path,
+                                               const char *meta_path, const char *prefix, uint32_t ctb) {
+    if (!c || !raid_path || !meta_path || !prefix) return GLINT_ERR_INVALID_ARGUMENT;
+    glint_block_info bi;
+    glint_status st = glint_store_block_info(c, block, &bi);
+    if (st != GLINT_OK) return st;
+    const uint32_t C = bi.CTF_count, N = c->N;
+    const glint_store_info &info = bi.store;
+    std::vector<uint8_t> keys(info.key_bytes ? info.key_bytes : 1), bitmaps((size_t)C * kBitmapBytes),
+        obitmap(kBitmapBytes), okeys((size_t)16 * info.oversize_kv_count + 16);
+    std::vector<uint16_t> sids(N ? N : 1);
+    std::vector<glint_ctf_meta> ctfs(C ? C : 1);
+    std::vector<float> oboxes((size_t)4 * info.oversize_kv_count + 4);
+    st = glint_store_block_read(c, block, keys.data(), sids.data(), ctfs.data(), bitmaps.data(), okeys.data(),
+                                oboxes.data(), obitmap.data());
+    if (st != GLINT_OK) return st;
+    glint_store_view v;
+    std::memset(&v, 0, sizeof(v));
+    v.num_objects = N;
+    v.CTF_count = C;
+    v.keys = keys.data();
+    v.sids = sids.data();
+    v.ctfs = ctfs.data();
+    v.bitmaps = bitmaps.data();
+    v.oversize_keys = okeys.data();
+    v.oversize_boxes = oboxes.data();
+    v.oversize_bitmap = obitmap.data();
+    v.info = info;
+    std::string err;
+    st = write_store(v, Paths{raid_path, meta_path, prefix, ctb}, err, bi.times);
+    if (st != GLINT_OK) c->last_error = "block dump: " + err;
+    return st;
 }

@@ -373,6 +373,63 @@ glint_status glint_store_dump(glint_ctx *ctx, const char *raid_path, const char 
  * base the flush wrote there. */
 glint_status glint_store_load(glint_ctx *ctx, const char *raid_path, const char *meta_path, const char *prefix,
                               uint32_t ctb);
+/* the same for a block of ctf_count CTFs (a compacted block: merge_dump
+ * leaves the CTB record's CTF count zero, and the reference's loader takes
+ * the count from its configuration, tracing/workbench.cpp:677-681) */
+glint_status glint_store_load_ctfs(glint_ctx *ctx, const char *raid_path, const char *meta_path, const char *prefix,
+                                   uint32_t ctb, uint32_t ctf_count);
+
+/* ---- the blocks kept on the device ------------------------------------------
+ * Kept blocks are numbered from 0, the oldest (glint_store_blocks gives
+ * their number). */
+typedef struct glint_block_info {
+    uint32_t CTF_count;
+    uint32_t times[4];             /* the CTB record's start_time_min/max, end_time_min/max */
+    uint32_t reserved;
+    glint_store_info store;        /* key count and bytes, the oversize buffer's count and times,
+                                      end_time_min = base of the key end offsets */
+} glint_block_info;
+glint_status glint_store_block_info(glint_ctx *ctx, uint32_t block, glint_block_info *info);
+/* a kept block into host arrays (any may be NULL), sized as glint_store_read's
+ * with CTF_count from glint_store_block_info */
+glint_status glint_store_block_read(glint_ctx *ctx, uint32_t block, uint8_t *keys, uint16_t *sids,
+                                    glint_ctf_meta *ctfs, uint8_t *bitmaps, void *oversize_keys,
+                                    float *oversize_boxes, uint8_t *oversize_bitmap);
+/* a kept block into files, in the layout of glint_store_write */
+glint_status glint_store_block_dump(glint_ctx *ctx, uint32_t block, const char *raid_path, const char *meta_path,
+                                    const char *prefix, uint32_t ctb);
+
+/* ---- compaction of kept blocks ------------------------------------------------
+ * merge_dump (tools/compaction.cpp:729-1215) merges `count` consecutive
+ * blocks into one of split_num^2 CTFs: every CTF key is parsed, objects are
+ * re-partitioned by STR over the middle of their boxes across all merged
+ * blocks, each object's keys are ordered by target, CTF limits, bit widths,
+ * bitmaps and packed keys are rebuilt, and the oversize buffers are merged in
+ * key order.  Its quirks are kept: the last object of the STR order keeps
+ * sid 2 and no CTF keys, object lists that STR leaves short are filled with
+ * object 0 (whose keys then repeat at the front of those CTFs), and the packed
+ * end is the absolute end plus the new CTFs' end_time_min.  Where the
+ * reference leaves the order of equivalent objects or keys to std::sort,
+ * this keeps them in a stable order (object id; source block and position).
+ * The new block takes the place of the merged ones among the kept blocks.
+ * GLINT_ERR_UNSUPPORTED (GLINT_EF_STORE_DOMAIN) where merge_dump leaves its
+ * domain: no CTF key, a partition size that underflows (too few objects for
+ * split_num), a CTF whose bits get_ctf_bits rejects, a key whose object id
+ * is beyond num_objects, or a source oversize buffer out of key order. */
+typedef struct glint_compact_info {
+    uint32_t CTF_count;            /* split_num^2 */
+    uint32_t blocks;               /* blocks merged */
+    uint64_t kv_count;             /* keys in the new CTFs */
+    uint64_t key_bytes;
+    uint64_t padding;              /* object-list entries filled with object 0 */
+    uint32_t oversize_kv_count;
+    uint32_t sid_count;            /* objects placed in CTFs */
+    uint32_t x_part, y_part;       /* merge_dump's partition sizes */
+    float ms;                      /* device time of the merge */
+    uint32_t reserved;
+} glint_compact_info;
+glint_status glint_store_compact(glint_ctx *ctx, uint32_t first, uint32_t count, uint32_t split_num,
+                                 glint_compact_info *info);
 
 /* ---- contact-trace queries over the flushed store ---------------------------
  * The reference reads its store per object (id_search_in_CTB,
