@@ -10,7 +10,9 @@ the reference's loop does).  Both forms produce bit-identical meetings;
 "plain" runs the reference's FP64 test on every candidate pair, "tuned"
 screens pairs in FP32 with a guard band first.  After the steps, the serving
 form answers a Poisson stream of contact-trace queries against the flushed
-store (p50/p99 latency, queries/s).
+store (p50/p99 latency, queries/s), and the compaction leg merges the kept
+blocks into one of 56^2 CTFs (merge_dump), with a 500k-object sample merged
+by the device and by the oracle on the host and compared bit for bit.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
                     [--objects N] [--mode both|plain|tuned]
@@ -63,6 +65,10 @@ def parse():
     p.add_argument("--serve-seconds", type=float, default=6.0)
     p.add_argument("--serve-rate", type=float, default=200.0)
     p.add_argument("--no-serve", action="store_true")
+    p.add_argument("--compact-split", type=int, default=56,
+                   help="split_num of the compaction leg (the reference tool merges into 56^2 = 3136 CTFs)")
+    p.add_argument("--compact-sample-objects", type=int, default=500_000)
+    p.add_argument("--no-compact", action="store_true")
     p.add_argument("--workload", default="step10m", choices=["step10m", "batch64", "skew50m"],
                    help="step10m: the headline line; batch64 / skew50m: the batching and precision forms")
     p.add_argument("--regions", type=int, default=64)
@@ -453,6 +459,73 @@ def serving(args, bench, N, t_hi):
                                  "queries": len(two)}}
 
 
+def compaction(args, bench):
+    """merge_dump at full scale: every kept block of the timed run merged into
+    one block of split_num^2 CTFs on the device (glint_store_compact)."""
+    nb = bench.store_blocks()
+    if nb < 2:
+        return None
+    infos = [bench.block_info(i).store for i in range(nb)]
+    src_keys = sum(int(i.kv_count) for i in infos)
+    src_bytes = sum(int(i.key_bytes) for i in infos)
+    t0 = time.perf_counter()
+    try:
+        info = bench.compact(0, nb, args.compact_split)
+    except Exception as e:  # a domain error of the reference's merge is reported, not fatal
+        return {"blocks": nb, "split_num": args.compact_split, "error": str(e)}
+    wall = (time.perf_counter() - t0) * 1000.0
+    ms = info["ms"]
+    return {"blocks": nb, "split_num": args.compact_split, "ctfs": info["CTF_count"], "source_keys": src_keys,
+            "keys": info["kv_count"], "oversize_keys": info["oversize_kv_count"], "padding": info["padding"],
+            "placed_objects": info["sid_count"], "ms": ms, "wall_ms": wall,
+            "source_keys_per_s": src_keys / (ms / 1000.0),
+            "packed_GBps": (src_bytes + info["key_bytes"]) / (ms / 1000.0) / 1e9,
+            "note": "ms: CUDA events around the merge on the context's stream (host steps between its launches "
+                    "included); packed_GBps: source and merged packed key bytes over that time"}
+
+
+def compaction_sample(args, local):
+    """The same merge on a sample the host can check: the generator at
+    --compact-sample-objects objects, three flushed windows, all blocks merged
+    on the device and by the oracle's C restatement (one thread), whose
+    results must be equal bit for bit.  A flush every 12 steps: earlier
+    windows leave CTFs without keys, outside the reference's flush domain."""
+    import glint_pipeline_gb300 as gp
+    from glint_pipeline_gb300.tracegen import SEED_SCALE, TraceGenerator
+    from oracle.bindings import compact_blocks
+    n = args.compact_sample_objects
+    if n <= 0:
+        return None
+    steps = 36
+    g = TraceGenerator(SEED_SCALE + 0x5a5a, n)
+    box, pts = g.box(), g.steps(steps)
+    cfg = gp.Configuration(num_objects=n, num_meeting_buckets=next_pow2(64 * n), device=local, store_keep=16)
+    b = gp.DeviceBench(cfg, box, pts[0])
+    try:
+        for t in range(steps):
+            b.step(pts[t], t)
+            if t % 12 == 11:
+                b.flush()
+        nb = b.store_blocks()
+        blocks = [b.block(i) for i in range(nb)]
+        src_keys = sum(int(x["ctfs"]["CTF_kv_capacity"].sum()) for x in blocks)
+        split = max(2, min(args.compact_split, int(round((n / 60.0) ** (1.0 / 3.0)))))
+        t0 = time.perf_counter()
+        rc, want = compact_blocks(blocks, n, box, split)
+        cpu_s = time.perf_counter() - t0
+        if rc != 0:
+            return {"objects": n, "blocks": nb, "split_num": split, "error": f"oracle rc {rc}"}
+        info = b.compact(0, nb, split)
+        got = b.block(0)
+        equal = rc == 0 and all(np.array_equal(got[k], want[k]) for k in ("sids", "keys", "bitmaps", "o_keys"))
+        equal = equal and np.array_equal(got["ctfs"].view(np.uint8), want["ctfs"].view(np.uint8))
+        return {"objects": n, "blocks": nb, "split_num": split, "source_keys": src_keys, "gpu_ms": info["ms"],
+                "cpu_ms": cpu_s * 1000.0, "cpu": "oracle C restatement, 1 thread", "bit_exact": bool(equal),
+                "gpu_source_keys_per_s": src_keys / (info["ms"] / 1000.0), "cpu_source_keys_per_s": src_keys / cpu_s}
+    finally:
+        b.close()
+
+
 def next_pow2(v):
     p = 1
     while p < v:
@@ -753,16 +826,20 @@ def main():
 
     modes = ["tuned", "plain"] if args.mode == "both" else [args.mode]
     forms = {}
-    serve = None
+    serve = compact = None
     for m in modes:
         forms[m] = run_form(args, m, N, local, pg, world, box, first, pb, ob, dbuf, step_bytes, rt)
         b = forms[m].pop("_bench")
         if m == modes[0] and not args.no_serve:
             serve = serving(args, b, N, total)
+        if m == modes[0] and not args.no_compact:
+            compact = compaction(args, b)
         b.close()
     rt.cudaFree(dbuf)
     head = forms[modes[0]]
     cpu = cpu_baseline(args) if (rank == 0 and world == 1 and not args.no_cpu) else None
+    if compact is not None and rank == 0 and world == 1 and not args.no_cpu:
+        compact["sample"] = compaction_sample(args, local)
     if rank == 0:
         line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
                 "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -773,7 +850,7 @@ def main():
                            "objects": N, "buckets": args.buckets, "form": modes[0],
                            "l2": "inputs larger than L2 (160 MB of points per step, 34 GB table)"},
                 "roofline": roofline(head, N, args.buckets, modes[0]), "clocks": head["clocks"], "e2e": head["e2e"], "cpu_baseline": cpu,
-                "gpu_launches": head["gpu_launches"], "serving": serve,
+                "gpu_launches": head["gpu_launches"], "serving": serve, "compaction": compact,
                 "forms": {m: {k: v for k, v in f.items()} for m, f in forms.items()}}
         print(json.dumps(line), flush=True)
 

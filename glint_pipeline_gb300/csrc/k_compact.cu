@@ -108,7 +108,11 @@ __global__ void __launch_bounds__(256) k_cmp_parse(const SrcBlock *__restrict__ 
         v >>= m.duration_bit;
         r.target = (uint32_t)(v & ((1ull << m.id_bit) - 1));
         v >>= m.id_bit;
-        r.oid = (uint32_t)v;
+        /* the flush writes its whole (sid, oid) field above the target, and
+         * the packed bytes keep sid bits when key_bit rounds up past the id
+         * (N > 2^19): the id is read with id_bit bits, as
+         * CTF::ctf_get_key_oid (tracing/step_merge.cpp:331-333) reads it */
+        r.oid = (uint32_t)(v & ((1ull << m.id_bit) - 1));
         r.end += m.end_time_min;
         /* CTF::new_parse_mbr_f_box: double arithmetic, float results */
         const uint64_t me = (1ull << m.edge_bit) - 1, my = (1ull << m.low_y_bit) - 1, mx = (1ull << m.low_x_bit) - 1;

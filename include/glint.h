@@ -411,6 +411,11 @@ glint_status glint_store_block_dump(glint_ctx *ctx, uint32_t block, const char *
  * end is the absolute end plus the new CTFs' end_time_min.  Where the
  * reference leaves the order of equivalent objects or keys to std::sort,
  * this keeps them in a stable order (object id; source block and position).
+ * Keys are parsed as CTF::parse_key does, except that the object id is read
+ * with id_bit bits, as the reference's readers read it: the flush writes its
+ * whole (sid, oid) field above the target, so with more than 2^19 objects the
+ * packed bytes can keep sid bits above the id, which parse_key would take
+ * into the id (and merge_dump would index past its object arrays).
  * The new block takes the place of the merged ones among the kept blocks.
  * GLINT_ERR_UNSUPPORTED (GLINT_EF_STORE_DOMAIN) where merge_dump leaves its
  * domain: no CTF key, a partition size that underflows (too few objects for

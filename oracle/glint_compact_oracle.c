@@ -85,7 +85,13 @@ static void parse_key(const go_ctf_meta *c, const uint8_t *p, gc_rec *r, uint64_
     k >>= c->duration_bit;
     r->target = (uint32_t)(k & ((1ull << c->id_bit) - 1));
     k >>= c->id_bit;
-    r->oid = (uint32_t)k;
+    /* parse_key keeps every bit above the target as the object id, but the
+     * flush writes the whole 38-bit (sid, oid) field there (extract_fields,
+     * cuda/cuda_util.cuh:164-169), so the packed bytes can hold sid bits above
+     * the id (key_bit rounds up, N > 2^19) and merge_dump would index past
+     * its object arrays; the id is read as the reference's readers read it,
+     * id_bit bits (CTF::ctf_get_key_oid, tracing/step_merge.cpp:331-333) */
+    r->oid = (uint32_t)(k & ((1ull << c->id_bit) - 1));
 }
 
 /* CTF::new_parse_mbr_f_box (tracing/step_merge.cpp:381-398): double

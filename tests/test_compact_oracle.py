@@ -113,6 +113,39 @@ def test_compacted_layout(split_num):
     assert res["kv_count"] == int(src.sum()) - sum(int(src[o]) for o in last) + extra0
 
 
+def test_bits_above_the_id_are_not_the_id():
+    """the flush writes its (sid, oid) field whole above the target, so a
+    packed key keeps sid bits above the id where key_bit rounds up past it
+    (N > 2^19); they are read as the reference's readers read the id
+    (CTF::ctf_get_key_oid), and the merge does not change"""
+    box, blocks = source_blocks(name="reach_8k", steps=40, flush_at=(19, 39))
+    n = blocks[0][1]["sids"].shape[0]
+    bs = [b for _, b in blocks]
+    rc, want = compact_blocks(bs, n, box, 3)
+    assert rc == 0
+    marked = []
+    for b in bs:
+        b = dict(b)
+        keys = b["keys"].copy()
+        off = 0
+        for m in b["ctfs"]:
+            kb, cnt = int(m["key_bit"]) // 8, int(m["CTF_kv_capacity"])
+            top = 2 * int(m["id_bit"]) + int(m["duration_bit"]) + int(m["end_bit"]) + int(m["mbr_bit"])
+            if int(m["key_bit"]) > top and cnt:
+                raw = keys[off:off + kb * cnt].reshape(cnt, kb)
+                for r in raw:
+                    v = int.from_bytes(r.tobytes(), "little") | (1 << top)   # a sid bit above the id
+                    r[:] = np.frombuffer(v.to_bytes(kb, "little"), np.uint8)
+            off += kb * cnt
+        assert not np.array_equal(keys, b["keys"])
+        b["keys"] = keys
+        marked.append(b)
+    rc2, got = compact_blocks(marked, n, box, 3)
+    assert rc2 == 0
+    for k in ("sids", "keys", "bitmaps", "o_keys"):
+        np.testing.assert_array_equal(got[k], want[k])
+
+
 def test_domain_errors():
     box, blocks = source_blocks(name="reach_8k", steps=40, flush_at=(19, 39))
     n = blocks[0][1]["sids"].shape[0]
