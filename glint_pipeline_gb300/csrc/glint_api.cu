@@ -184,6 +184,10 @@ void free_all(glint_ctx *c) {
         if (p) cudaFree(p);
     flush_free(c);
     store_blocks_free(c);
+    if (c->compact_pool) {
+        if (c->stream) cudaStreamSynchronize(c->stream);
+        cudaMemPoolDestroy(c->compact_pool);
+    }
     server_free_default(c);
     servers_detach(c);
     if (c->h_cnt) cudaFreeHost(c->h_cnt);

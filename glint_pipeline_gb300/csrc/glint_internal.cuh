@@ -230,6 +230,7 @@ struct glint_ctx {
     uint64_t store_kv = 0;
     uint32_t flushes = 0;
     std::vector<glint::StoreBlock> ctbs;   /* flushed blocks kept for queries, oldest first */
+    cudaMemPool_t compact_pool = nullptr;  /* compaction scratch; stays mapped between merges */
     glint_server *server = nullptr;        /* the default server behind glint_query_batch */
     std::vector<glint_server *> servers;   /* every live server on this context */
     cudaEvent_t flush_ev[2];

@@ -52,7 +52,9 @@ struct SrcBlock {
     const glint_ctf_meta *ctfs;
     const unsigned long long *key_index, *byte_index;
     const uint16_t *sids;
+    const uint3 *toff;          /* [C] offsets of each CTF's decode tables */
     unsigned long long base;    /* first record of the block */
+    unsigned long long key_bytes;
     uint32_t C, pad;
 };
 
@@ -83,8 +85,50 @@ __device__ inline uint32_t last_le(const unsigned long long *a, uint32_t n, unsi
     return lo;
 }
 
+/* decode tables of one CTF (new_parse_mbr_f_box, tracing/step_merge.cpp:381-398):
+ * the low corner's coordinates for every quantised value, rounded to float,
+ * and the edge offsets in double; the box is then b0 = T0[l0], b2 =
+ * float(double(b0) + E[x]), the reference's operations in its order */
+__global__ void k_cmp_tables(const glint_ctf_meta *__restrict__ ctfs, const uint3 *__restrict__ toff,
+                             float *__restrict__ tf, double *__restrict__ td) {
+    const uint32_t j = blockIdx.x;
+    const glint_ctf_meta m = ctfs[j];
+    const uint3 o = toff[j];
+    const uint64_t me = (1ull << m.edge_bit) - 1, my = (1ull << m.low_y_bit) - 1, mx = (1ull << m.low_x_bit) - 1;
+    const float ex = __fsub_rn(m.ctf_mbr[2], m.ctf_mbr[0]), ey = __fsub_rn(m.ctf_mbr[3], m.ctf_mbr[1]);
+    const float le = ex < ey ? ey : ex;
+    for (uint64_t v = threadIdx.x; v <= mx; v += blockDim.x)
+        tf[o.x + v] = __double2float_rn(
+            __dadd_rn((double)m.ctf_mbr[0], __dmul_rn(__ddiv_rn(__ull2double_rn(v), __ull2double_rn(mx)), (double)ex)));
+    for (uint64_t v = threadIdx.x; v <= my; v += blockDim.x)
+        tf[o.y + v] = __double2float_rn(
+            __dadd_rn((double)m.ctf_mbr[1], __dmul_rn(__ddiv_rn(__ull2double_rn(v), __ull2double_rn(my)), (double)ey)));
+    for (uint64_t v = threadIdx.x; v <= me; v += blockDim.x)
+        td[o.z + v] = __dmul_rn(__ddiv_rn(__ull2double_rn(v), __ull2double_rn(me)), (double)le);
+}
+
+/* kb <= 16 little-endian bytes at p; whole words where they stay inside the
+ * buffer */
+__device__ inline u128 load_key(const uint8_t *p, uint32_t kb, const uint8_t *end) {
+    const uintptr_t a = (uintptr_t)p;
+    const uint64_t *w = (const uint64_t *)(a & ~(uintptr_t)7);
+    const uint32_t sh = (uint32_t)(a & 7) * 8;
+    u128 v;
+    if ((const uint8_t *)(w + 3) <= end) {
+        const uint64_t w0 = w[0], w1 = w[1];
+        v = ((u128)w1 << 64 | w0) >> sh;
+        if (sh) v |= (u128)w[2] << (128 - sh);
+    } else {
+        v = 0;
+        for (uint32_t t = 0; t < kb; ++t) v |= (u128)p[t] << (8 * t);
+        return v;
+    }
+    return kb < 16 ? v & (((u128)1 << (8 * kb)) - 1) : v;
+}
+
 __global__ void __launch_bounds__(256) k_cmp_parse(const SrcBlock *__restrict__ src, uint32_t nsrc, uint64_t R,
-                                                   uint32_t N, Rec *__restrict__ recs,
+                                                   uint32_t N, const float *__restrict__ tf,
+                                                   const double *__restrict__ td, Rec *__restrict__ recs,
                                                    unsigned long long *__restrict__ skey, uint32_t *__restrict__ sval,
                                                    unsigned long long *__restrict__ counters) {
     for (uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; g < R; g += (uint64_t)gridDim.x * blockDim.x) {
@@ -95,9 +139,7 @@ __global__ void __launch_bounds__(256) k_cmp_parse(const SrcBlock *__restrict__ 
         const uint32_t j = last_le(b.key_index, b.C, k);
         const glint_ctf_meta m = b.ctfs[j];
         const uint32_t kb = m.key_bit / 8;
-        const uint8_t *p = b.keys + b.byte_index[j] + (k - b.key_index[j]) * kb;
-        u128 v = 0;
-        for (uint32_t t = 0; t < kb; ++t) v |= (u128)p[t] << (8 * t);
+        u128 v = load_key(b.keys + b.byte_index[j] + (k - b.key_index[j]) * kb, kb, b.keys + b.key_bytes);
         /* CTF::parse_key */
         uint64_t vm = (uint64_t)(v & (((u128)1 << m.mbr_bit) - 1));
         v >>= m.mbr_bit;
@@ -114,7 +156,8 @@ __global__ void __launch_bounds__(256) k_cmp_parse(const SrcBlock *__restrict__ 
          * CTF::ctf_get_key_oid (tracing/step_merge.cpp:331-333) reads it */
         r.oid = (uint32_t)(v & ((1ull << m.id_bit) - 1));
         r.end += m.end_time_min;
-        /* CTF::new_parse_mbr_f_box: double arithmetic, float results */
+        /* the box from the CTF's decode tables */
+        const uint3 o = b.toff[j];
         const uint64_t me = (1ull << m.edge_bit) - 1, my = (1ull << m.low_y_bit) - 1, mx = (1ull << m.low_x_bit) - 1;
         const uint64_t y = vm & me;
         vm >>= m.edge_bit;
@@ -123,16 +166,9 @@ __global__ void __launch_bounds__(256) k_cmp_parse(const SrcBlock *__restrict__ 
         const uint64_t l1 = vm & my;
         vm >>= m.low_y_bit;
         const uint64_t l0 = vm & mx;
-        const float ex = __fsub_rn(m.ctf_mbr[2], m.ctf_mbr[0]), ey = __fsub_rn(m.ctf_mbr[3], m.ctf_mbr[1]);
-        const float le = ex < ey ? ey : ex;
-        const float b0 = __double2float_rn(
-            __dadd_rn((double)m.ctf_mbr[0], __dmul_rn(__ddiv_rn(__ull2double_rn(l0), __ull2double_rn(mx)), (double)ex)));
-        const float b1 = __double2float_rn(
-            __dadd_rn((double)m.ctf_mbr[1], __dmul_rn(__ddiv_rn(__ull2double_rn(l1), __ull2double_rn(my)), (double)ey)));
-        const float b2 = __double2float_rn(
-            __dadd_rn((double)b0, __dmul_rn(__ddiv_rn(__ull2double_rn(x), __ull2double_rn(me)), (double)le)));
-        const float b3 = __double2float_rn(
-            __dadd_rn((double)b1, __dmul_rn(__ddiv_rn(__ull2double_rn(y), __ull2double_rn(me)), (double)le)));
+        const float b0 = tf[o.x + l0], b1 = tf[o.y + l1];
+        const float b2 = __double2float_rn(__dadd_rn((double)b0, td[o.z + x]));
+        const float b3 = __double2float_rn(__dadd_rn((double)b1, td[o.z + y]));
         r.box = make_float4(b0, b1, b2, b3);
         recs[g] = r;
         sval[g] = (uint32_t)g;
@@ -147,6 +183,13 @@ __global__ void __launch_bounds__(256) k_cmp_parse(const SrcBlock *__restrict__ 
     }
 }
 
+/* the records in sorted order */
+__global__ void k_cmp_permute(uint64_t n, const uint32_t *__restrict__ sidx, const Rec *__restrict__ recs,
+                              Rec *__restrict__ out) {
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < n; p += (uint64_t)gridDim.x * blockDim.x)
+        out[p] = recs[sidx[p]];
+}
+
 /* each object's run [first, end) in the sorted order */
 __global__ void k_cmp_runs(const unsigned long long *__restrict__ skey, uint64_t n, uint32_t *__restrict__ rfirst,
                            uint32_t *__restrict__ rend) {
@@ -157,16 +200,18 @@ __global__ void k_cmp_runs(const unsigned long long *__restrict__ skey, uint64_t
     }
 }
 
-__device__ inline unsigned long long order_key(double v) {
-    if (v == 0.0) v = 0.0; /* -0 and +0 compare equal */
-    const unsigned long long u = (unsigned long long)__double_as_longlong(v);
-    return (u >> 63) ? ~u : (u | (1ull << 63));
+/* ave_loc holds a float widened to double, so the float's order is the
+ * double's; -0 and +0 compare equal */
+__device__ inline unsigned long long order_key(float v) {
+    if (v == 0.0f) v = 0.0f;
+    const uint32_t u = __float_as_uint(v);
+    return (u >> 31) ? (~u & 0xffffffffu) : (u | 0x80000000u);
 }
 
 /* per object: key count, box (f_box::update), start limits, class (0 none, 1
  * oversize in a source block, 2 CTF keys) and the middles of its box */
 __global__ void k_cmp_objects(uint32_t N, const uint32_t *__restrict__ rfirst, const uint32_t *__restrict__ rend,
-                              const uint32_t *__restrict__ sidx, const Rec *__restrict__ recs,
+                              const Rec *__restrict__ prec,
                               const SrcBlock *__restrict__ src, uint32_t nsrc, uint32_t *__restrict__ nkeys,
                               float4 *__restrict__ obox, uint2 *__restrict__ ostart, uint8_t *__restrict__ cls,
                               uint32_t *__restrict__ is2, unsigned long long *__restrict__ xkey,
@@ -177,7 +222,7 @@ __global__ void k_cmp_objects(uint32_t N, const uint32_t *__restrict__ rfirst, c
         float4 a = make_float4(100000.0f, 100000.0f, -100000.0f, -100000.0f);
         uint32_t smin = 1u << 30, smax = 1u;
         for (uint32_t p = f; p < e; ++p) {
-            const Rec r = recs[sidx[p]];
+            const Rec r = prec[p];
             if (a.x > r.box.x) a.x = r.box.x;
             if (a.z < r.box.z) a.z = r.box.z;
             if (a.y > r.box.y) a.y = r.box.y;
@@ -195,9 +240,9 @@ __global__ void k_cmp_objects(uint32_t N, const uint32_t *__restrict__ rfirst, c
         ostart[o] = make_uint2(smin, smax);
         cls[o] = c;
         is2[o] = c == 2;
-        /* ave_loc: float halves added in float, widened to double */
-        xkey[o] = order_key((double)__fadd_rn(__fdiv_rn(a.x, 2.0f), __fdiv_rn(a.z, 2.0f)));
-        ykey[o] = order_key((double)__fadd_rn(__fdiv_rn(a.y, 2.0f), __fdiv_rn(a.w, 2.0f)));
+        /* ave_loc: float halves added in float (then widened to double) */
+        xkey[o] = order_key(__fadd_rn(__fdiv_rn(a.x, 2.0f), __fdiv_rn(a.z, 2.0f)));
+        ykey[o] = order_key(__fadd_rn(__fdiv_rn(a.y, 2.0f), __fdiv_rn(a.w, 2.0f)));
     }
 }
 
@@ -233,18 +278,33 @@ __global__ void k_cmp_parts(uint32_t S, uint32_t split, uint32_t x_part, uint32_
     }
 }
 
-/* positions [0, split_index) get their CTF (merge_dump :900-917); keys for
- * the (CTF, oid) order of the placed objects */
+/* positions [0, split_index) get their CTF (merge_dump :900-917) */
 __global__ void k_cmp_assign(uint32_t split, uint32_t x_part, uint32_t y_part, uint32_t s,
                              const uint32_t *__restrict__ yv, const uint32_t *__restrict__ xorder,
-                             uint16_t *__restrict__ sids, unsigned long long *__restrict__ ck, uint32_t *__restrict__ cv) {
+                             uint16_t *__restrict__ sids, uint32_t *__restrict__ ctf_of) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < split; i += gridDim.x * blockDim.x) {
         const uint32_t o = xorder[yv[i]];
         const uint32_t xi = i / x_part, yi = (i % x_part) / y_part;
         const uint32_t c = xi * s + yi;
         sids[o] = (uint16_t)(c + 2);
-        ck[i] = ((unsigned long long)c << kOidBit) | o;
-        cv[i] = o;
+        ctf_of[o] = c;
+    }
+}
+
+__global__ void k_cmp_placed(uint32_t N, const uint32_t *__restrict__ ctf_of, uint32_t *__restrict__ flag) {
+    for (uint32_t o = blockIdx.x * blockDim.x + threadIdx.x; o < N; o += gridDim.x * blockDim.x)
+        flag[o] = ctf_of[o] != 0xffffffffu;
+}
+
+/* the placed objects in id order, keyed by CTF (a stable sort by CTF then
+ * gives the (CTF, oid) order of the CTFs' object lists) */
+__global__ void k_cmp_plist(uint32_t N, const uint32_t *__restrict__ ctf_of, const uint32_t *__restrict__ pos,
+                            unsigned long long *__restrict__ ck, uint32_t *__restrict__ cv) {
+    for (uint32_t o = blockIdx.x * blockDim.x + threadIdx.x; o < N; o += gridDim.x * blockDim.x) {
+        const uint32_t c = ctf_of[o];
+        if (c == 0xffffffffu) continue;
+        ck[pos[o]] = c;
+        cv[pos[o]] = o;
     }
 }
 
@@ -296,71 +356,113 @@ struct PackArgs {
     const unsigned long long *key_index, *byte_index; /* [C + 1] */
     const unsigned long long *cstart;                  /* [C + 1] object-list start of each CTF */
     const unsigned long long *pad;                     /* [C] object-list entries filled with object 0 */
+    const unsigned long long *padk;                    /* [C + 1] prefix of pad * n0: the repeated keys */
     const uint32_t *escan;                             /* [placed + 1] keys before each listed object */
-    const uint32_t *olist, *rfirst, *sidx;
-    const Rec *recs;
+    const uint32_t *posof, *rfirst, *ctf_of;
+    const unsigned long long *obase;                   /* [N] a placed object's first key in the block */
+    const Rec *prec;                                   /* records in (oid, target) order */
     uint8_t *out;
     uint32_t *bits;
     unsigned long long *counters;
-    uint64_t kv;
+    uint64_t n;                                        /* records (or repeated keys) to emit */
     uint32_t C, n0;
 };
 
-/* one thread per output key: which object's key it is, its bitmap cells
- * and its packed bytes */
-__global__ void __launch_bounds__(256) k_cmp_pack(PackArgs a) {
-    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < a.kv;
-         t += (uint64_t)gridDim.x * blockDim.x) {
-        const uint32_t c = last_le(a.key_index, a.C, t);
-        const glint_ctf_meta m = a.ctfs[c];
-        const unsigned long long q = t - a.key_index[c];
-        const unsigned long long padk = a.pad[c] * a.n0;
-        uint64_t pos;
-        if (q < padk) {
-            pos = a.rfirst[0] + q % a.n0;
-        } else {
-            const unsigned long long q2 = q - padk;
-            const unsigned long long j0 = a.cstart[c], j1 = a.cstart[c + 1];
-            const uint32_t e0 = a.escan[j0];
-            unsigned long long lo = j0, hi = j1; /* escan[lo] - e0 <= q2 < escan[lo + 1] - e0 */
-            while (hi - lo > 1) {
-                const unsigned long long mid = (lo + hi) >> 1;
-                if (a.escan[mid] - e0 <= q2) lo = mid;
-                else hi = mid;
-            }
-            pos = a.rfirst[a.olist[lo]] + (q2 - (a.escan[lo] - e0));
-        }
-        const Rec r = a.recs[a.sidx[pos]];
-        /* bitmap cells (:1018-1038), inside the CTF's grid */
-        const float ex = __fsub_rn(m.ctf_mbr[2], m.ctf_mbr[0]), ey = __fsub_rn(m.ctf_mbr[3], m.ctf_mbr[1]);
-        const float xg = (float)m.x_grid, yg = (float)m.y_grid;
-        const uint32_t l0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(r.box.x, m.ctf_mbr[0]), ex), xg));
-        const uint32_t l1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(r.box.y, m.ctf_mbr[1]), ey), yg));
-        const uint32_t h0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(r.box.z, m.ctf_mbr[0]), ex), xg));
-        const uint32_t h1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(r.box.w, m.ctf_mbr[1]), ey), yg));
-        uint32_t *bits = a.bits + (uint64_t)c * (kBitBytes / 4);
-        uint64_t cells = 0;
-        for (uint32_t mx = l0; mx <= h0 && mx < m.x_grid; ++mx)
-            for (uint32_t ny = l1; ny <= h1 && ny < m.y_grid; ++ny) {
-                if (++cells > kCellLoopMax) {
-                    atomicAdd(&a.counters[kErrCells], 1ull);
-                    mx = h0;
-                    break;
-                }
-                const uint32_t pb = mx + ny * m.x_grid;
-                const uint32_t bit = 1u << (pb & 31);
-                if (!(__ldcg(&bits[pb >> 5]) & bit)) atomicOr(&bits[pb >> 5], bit);
-            }
-        /* the key (:1049-1060); the end is made absolute once more */
-        const u128 vm = serialize_box(r.box, m);
-        const u128 end = (u128)r.end + m.end_time_min;
-        const u128 key = ((u128)r.oid << (m.id_bit + m.duration_bit + m.end_bit + m.mbr_bit)) +
-                         ((u128)r.target << (m.duration_bit + m.end_bit + m.mbr_bit)) +
-                         ((u128)r.duration << (m.end_bit + m.mbr_bit)) + (end << m.mbr_bit) + vm;
-        const uint32_t kb = m.key_bit / 8;
-        uint8_t *o = a.out + a.byte_index[c] + q * kb;
-        for (uint32_t j = 0; j < kb; ++j) o[j] = (uint8_t)(key >> (8 * j));
+/* every placed object's records into output order (a placed object's keys
+ * follow object 0's repeats and the keys of the CTF's objects before it),
+ * whole 32-byte records so the scattered writes fill their sectors */
+__global__ void __launch_bounds__(256) k_cmp_place(PackArgs a, Rec *__restrict__ out) {
+    for (uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; p < a.n;
+         p += (uint64_t)gridDim.x * blockDim.x) {
+        const Rec r = a.prec[p];
+        if (a.ctf_of[r.oid] == 0xffffffffu) continue; /* the object STR leaves unplaced */
+        out[a.obase[r.oid] + (p - a.rfirst[r.oid])] = r;
     }
+}
+
+/* object 0's repeats at the front of the CTFs whose object lists STR leaves
+ * short */
+__global__ void __launch_bounds__(256) k_cmp_place_pad(PackArgs a, Rec *__restrict__ out) {
+    for (uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; t < a.n;
+         t += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t c = last_le(a.padk, a.C, t);
+        const unsigned long long q = t - a.padk[c];
+        out[a.key_index[c] + q] = a.prec[a.rfirst[0] + q % a.n0];
+    }
+}
+
+/* one block per chunk of a CTF's keys, in output order: consecutive threads
+ * write consecutive packed keys, and the chunk's bitmap cells (:1018-1038)
+ * are set in shared memory and OR-ed into the CTF's bitmap once */
+constexpr uint32_t kPackChunk = 16384;
+__global__ void __launch_bounds__(256) k_cmp_pack(PackArgs a, const Rec *__restrict__ ordered,
+                                                  const uint2 *__restrict__ chunks) {
+    __shared__ uint32_t sbits[kBitBytes / 4];
+    __shared__ uint8_t stage[8][32 * 16];  /* each warp's 32 packed keys */
+    const uint2 ch = chunks[blockIdx.x];   /* (CTF, first key of the chunk within it) */
+    const uint32_t c = ch.x;
+    const glint_ctf_meta m = a.ctfs[c];
+    const unsigned long long k0 = a.key_index[c], k1 = a.key_index[c + 1];
+    const unsigned long long b = k0 + ch.y, e = b + kPackChunk < k1 ? b + kPackChunk : k1;
+    const uint32_t words = ((uint32_t)m.x_grid * m.y_grid + 31) / 32;
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) sbits[i] = 0;
+    __syncthreads();
+    const float ex = __fsub_rn(m.ctf_mbr[2], m.ctf_mbr[0]), ey = __fsub_rn(m.ctf_mbr[3], m.ctf_mbr[1]);
+    const float xg = (float)m.x_grid, yg = (float)m.y_grid;
+    const uint32_t kb = m.key_bit / 8;
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint8_t *st = stage[w];
+    uint8_t *out = a.out + a.byte_index[c];
+    for (unsigned long long t0 = b + (unsigned long long)w * 32; t0 < e; t0 += blockDim.x) {
+        const unsigned long long t = t0 + lane;
+        const bool valid = t < e;
+        if (valid) {
+            const Rec r = ordered[t];
+            const uint32_t l0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(r.box.x, m.ctf_mbr[0]), ex), xg));
+            const uint32_t l1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(r.box.y, m.ctf_mbr[1]), ey), yg));
+            const uint32_t h0 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(r.box.z, m.ctf_mbr[0]), ex), xg));
+            const uint32_t h1 = __float2uint_rz(__fmul_rn(__fdiv_rn(__fsub_rn(r.box.w, m.ctf_mbr[1]), ey), yg));
+            uint64_t cells = 0;
+            for (uint32_t mx = l0; mx <= h0 && mx < m.x_grid; ++mx)
+                for (uint32_t ny = l1; ny <= h1 && ny < m.y_grid; ++ny) {
+                    if (++cells > kCellLoopMax) {
+                        atomicAdd(&a.counters[kErrCells], 1ull);
+                        mx = h0;
+                        break;
+                    }
+                    const uint32_t pb = mx + ny * m.x_grid, bit = 1u << (pb & 31);
+                    /* an object's keys share cells: most are set already */
+                    if (!(sbits[pb >> 5] & bit)) atomicOr(&sbits[pb >> 5], bit);
+                }
+            /* the key (:1049-1060), the end made absolute once more */
+            const u128 vm = serialize_box(r.box, m);
+            const u128 end = (u128)r.end + m.end_time_min;
+            const u128 key = ((u128)r.oid << (m.id_bit + m.duration_bit + m.end_bit + m.mbr_bit)) +
+                             ((u128)r.target << (m.duration_bit + m.end_bit + m.mbr_bit)) +
+                             ((u128)r.duration << (m.end_bit + m.mbr_bit)) + (end << m.mbr_bit) + vm;
+            for (uint32_t j = 0; j < kb; ++j) st[lane * kb + j] = (uint8_t)(key >> (8 * j));
+        }
+        __syncwarp();
+        /* the warp's keys are one run of bytes: aligned words, edge bytes */
+        const unsigned long long n = e - t0 < 32 ? e - t0 : 32;
+        const uint32_t len = (uint32_t)n * kb;
+        uint8_t *g = out + (t0 - k0) * kb;
+        const uint32_t head = (uint32_t)((4 - ((uintptr_t)g & 3)) & 3) < len ? (uint32_t)((4 - ((uintptr_t)g & 3)) & 3)
+                                                                                : len;
+        const uint32_t nw = (len - head) / 4, tail0 = head + nw * 4;
+        if ((uint32_t)lane < head) g[lane] = st[lane];
+        for (uint32_t q = lane; q < nw; q += 32) {
+            const uint8_t *sp = st + head + 4 * q;
+            *(uint32_t *)(g + head + 4 * q) =
+                (uint32_t)sp[0] | ((uint32_t)sp[1] << 8) | ((uint32_t)sp[2] << 16) | ((uint32_t)sp[3] << 24);
+        }
+        if ((uint32_t)lane < len - tail0) g[tail0 + lane] = st[tail0 + lane];
+        __syncwarp();
+    }
+    __syncthreads();
+    uint32_t *bits = a.bits + (uint64_t)c * (kBitBytes / 4);
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x)
+        if (sbits[i]) atomicOr(&bits[i], sbits[i]);
 }
 
 /* where each object's keys sit in the new block (its run of its own oid in
@@ -370,7 +472,8 @@ __global__ void k_cmp_index(uint32_t N, const uint16_t *__restrict__ sids, const
                             const uint32_t *__restrict__ posof, const unsigned long long *__restrict__ cstart,
                             const unsigned long long *__restrict__ key_index, const unsigned long long *__restrict__ pad,
                             const uint32_t *__restrict__ escan, const uint32_t *__restrict__ olist, uint32_t C,
-                            uint32_t n0, uint32_t *__restrict__ first, uint32_t *__restrict__ count) {
+                            uint32_t n0, uint32_t *__restrict__ first, uint32_t *__restrict__ count,
+                            unsigned long long *__restrict__ obase) {
     for (uint32_t o = blockIdx.x * blockDim.x + threadIdx.x; o < N; o += gridDim.x * blockDim.x) {
         const uint32_t sid = sids[o];
         uint32_t f = 0, n = 0;
@@ -381,6 +484,7 @@ __global__ void k_cmp_index(uint32_t N, const uint16_t *__restrict__ sids, const
             const unsigned long long padk = pad[c] * n0;
             if (member) {
                 f = (uint32_t)(key_index[c] + padk + (escan[j] - escan[cstart[c]]));
+                obase[o] = f;
                 n = nkeys[o];
                 if (o == 0) {
                     f = (uint32_t)key_index[c];
@@ -399,7 +503,7 @@ __global__ void k_cmp_index(uint32_t N, const uint16_t *__restrict__ sids, const
 /* the oversize buffers one after another, then the extra list as
  * (oid, target, duration, end) keys without sid bits (:1090-1097) */
 __global__ void k_cmp_ocat(const ulonglong2 *__restrict__ okeys, const float4 *__restrict__ oboxes, uint64_t n_src,
-                           const uint32_t *__restrict__ sidx, const Rec *__restrict__ recs, uint64_t extra_at,
+                           const Rec *__restrict__ prec, uint64_t extra_at,
                            uint64_t n_extra, unsigned long long *__restrict__ lo, unsigned long long *__restrict__ hi,
                            float4 *__restrict__ box, uint64_t at) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n_src + n_extra;
@@ -409,7 +513,7 @@ __global__ void k_cmp_ocat(const ulonglong2 *__restrict__ okeys, const float4 *_
             hi[at + i] = okeys[i].y;
             box[at + i] = oboxes[i];
         } else {
-            const Rec r = recs[sidx[extra_at + (i - n_src)]];
+            const Rec r = prec[extra_at + (i - n_src)];
             lo[at + i] = ((unsigned long long)r.duration << 32) | r.end;
             hi[at + i] = ((unsigned long long)r.oid << kOidBit) | r.target;
             box[at + i] = r.box;
@@ -430,10 +534,9 @@ __global__ void k_cmp_ocheck(const ulonglong2 *__restrict__ okeys, uint64_t n, u
 }
 
 /* the extra list (sorted by oid and target) in full-key order? */
-__global__ void k_cmp_xcheck(const uint32_t *__restrict__ sidx, const Rec *__restrict__ recs, uint64_t at, uint64_t n,
-                             unsigned long long *counters) {
+__global__ void k_cmp_xcheck(const Rec *__restrict__ prec, uint64_t at, uint64_t n, unsigned long long *counters) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x + 1; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-        const Rec a = recs[sidx[at + i - 1]], b = recs[sidx[at + i]];
+        const Rec a = prec[at + i - 1], b = prec[at + i];
         if (a.oid == b.oid && a.target == b.target &&
             (b.duration < a.duration || (b.duration == a.duration && b.end < a.end)))
             atomicAdd(&counters[kExtraOrder], 1ull);
@@ -505,15 +608,17 @@ __global__ void k_cmp_iota(uint64_t n, uint32_t *__restrict__ perm, const unsign
     }
 }
 
-/* device scratch released on the stream when the call returns */
+/* device scratch from the context's compaction pool, released on the stream
+ * when the call returns (the pool keeps it mapped for the next merge) */
 struct Scratch {
     cudaStream_t s;
+    cudaMemPool_t pool;
     std::vector<void *> ptrs;
     cudaError_t e = cudaSuccess;
-    explicit Scratch(cudaStream_t st) : s(st) {}
+    Scratch(cudaStream_t st, cudaMemPool_t p) : s(st), pool(p) {}
     template <class T> T *get(size_t n) {
         void *p = nullptr;
-        if (e == cudaSuccess) e = cudaMallocAsync(&p, (n ? n : 1) * sizeof(T), s);
+        if (e == cudaSuccess) e = cudaMallocFromPoolAsync(&p, (n ? n : 1) * sizeof(T), pool, s);
         if (e == cudaSuccess) ptrs.push_back(p);
         return static_cast<T *>(p);
     }
@@ -562,20 +667,56 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
     } ev;
     cudaEventRecord(ev.a, s);
 
-    /* the source blocks */
+    /* the source blocks and their CTFs' decode tables */
     std::vector<SrcBlock> hs(count);
-    uint64_t R = 0, O_src = 0;
+    std::vector<std::vector<uint3>> toffs(count);
+    uint64_t R = 0, O_src = 0, nf = 0, nd = 0;
     for (uint32_t i = 0; i < count; ++i) {
         const StoreBlock &b = c->ctbs[first + i];
-        hs[i] = SrcBlock{b.keys, b.ctfs, b.key_index, b.byte_index, b.sids, R, b.C, 0};
+        std::vector<glint_ctf_meta> m(b.C);
+        if (b.C && (e = cudaMemcpy(m.data(), b.ctfs, sizeof(glint_ctf_meta) * b.C, cudaMemcpyDeviceToHost)) !=
+                       cudaSuccess)
+            return cuda_fail(e, "source CTFs");
+        toffs[i].resize(b.C ? b.C : 1);
+        for (uint32_t j = 0; j < b.C; ++j) {
+            if (m[j].low_x_bit > 24 || m[j].low_y_bit > 24 || m[j].edge_bit > 24)
+                return domain("a source CTF's box bits beyond 24");
+            toffs[i][j] = make_uint3((uint32_t)nf, (uint32_t)(nf + (1ull << m[j].low_x_bit)), (uint32_t)nd);
+            nf += (1ull << m[j].low_x_bit) + (1ull << m[j].low_y_bit);
+            nd += 1ull << m[j].edge_bit;
+        }
+        hs[i] = SrcBlock{b.keys, b.ctfs, b.key_index, b.byte_index, b.sids, nullptr, R, b.key_bytes, b.C, 0};
         R += b.kv;
         O_src += b.o_count;
     }
     if (R >= (1ull << 32) - 1 || O_src + R >= (1ull << 32) - 1) return domain("more than 2^32 keys");
-    Scratch sc(s);
+    if (nf >= (1ull << 32) || nd >= (1ull << 32)) return domain("decode tables too large");
+    if (!c->compact_pool) {
+        cudaMemPoolProps props;
+        std::memset(&props, 0, sizeof(props));
+        props.allocType = cudaMemAllocationTypePinned;
+        props.location.type = cudaMemLocationTypeDevice;
+        props.location.id = c->device;
+        if ((e = cudaMemPoolCreate(&c->compact_pool, &props)) != cudaSuccess) {
+            c->compact_pool = nullptr;
+            return cuda_fail(e, "memory pool");
+        }
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(c->compact_pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    Scratch sc(s, c->compact_pool);
+    float *tf = sc.get<float>(nf);
+    double *td = sc.get<double>(nd);
+    for (uint32_t i = 0; i < count; ++i) {
+        uint3 *t = sc.get<uint3>(toffs[i].size());
+        if (sc.e != cudaSuccess) return cuda_fail(sc.e, "scratch");
+        cudaMemcpyAsync(t, toffs[i].data(), sizeof(uint3) * toffs[i].size(), cudaMemcpyHostToDevice, s);
+        hs[i].toff = t;
+        if (hs[i].C) k_cmp_tables<<<hs[i].C, 256, 0, s>>>(hs[i].ctfs, t, tf, td);
+    }
     SrcBlock *d_src = sc.get<SrcBlock>(count);
     unsigned long long *d_cnt = sc.get<unsigned long long>(kNumCounters);
-    Rec *recs = sc.get<Rec>(R);
+    Rec *recs = sc.get<Rec>(R), *prec = sc.get<Rec>(R);
     unsigned long long *skey = sc.get<unsigned long long>(R), *skey2 = sc.get<unsigned long long>(R);
     uint32_t *sval = sc.get<uint32_t>(R), *sval2 = sc.get<uint32_t>(R);
     const uint64_t sort_n = std::max<uint64_t>(std::max<uint64_t>(R, N), O_src + R);
@@ -594,7 +735,7 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
     cudaMemsetAsync(rend, 0, sizeof(uint32_t) * N, s);
 
     /* parse and order the keys */
-    if (R) k_cmp_parse<<<grid_for(R, 256), 256, 0, s>>>(d_src, count, R, N, recs, skey, sval, d_cnt);
+    if (R) k_cmp_parse<<<grid_for(R, 256), 256, 0, s>>>(d_src, count, R, N, tf, td, recs, skey, sval, d_cnt);
     if ((e = radix_sort_u64(skey, sval, skey2, sval2, R, 53, rs_tmp, scan_tmp, s)) != cudaSuccess)
         return cuda_fail(e, "key sort");
     unsigned long long hc[kNumCounters];
@@ -603,9 +744,10 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
         return cuda_fail(e, "parse");
     if (hc[kErrOid]) return domain("a key's object id is beyond num_objects");
     const uint64_t n_extra = hc[kExtraCount], R_ctf = R - n_extra;
+    if (R) k_cmp_permute<<<grid_for(R, 256), 256, 0, s>>>(R, sval, recs, prec);
     if (R_ctf) k_cmp_runs<<<grid_for(R_ctf, 256), 256, 0, s>>>(skey, R_ctf, rfirst, rend);
-    k_cmp_objects<<<grid_for(N, 256), 256, 0, s>>>(N, rfirst, rend, sval, recs, d_src, count, nkeys, obox, ostart,
-                                                   cls, is2, xkey, ykey);
+    k_cmp_objects<<<grid_for(N, 256), 256, 0, s>>>(N, rfirst, rend, prec, d_src, count, nkeys, obox, ostart, cls,
+                                                   is2, xkey, ykey);
 
     /* STR: the objects marked 2, by x middle */
     scan_u32(is2, pos2, N, scan_tmp, s);
@@ -623,15 +765,15 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
     unsigned long long *yk = sc.get<unsigned long long>(S);
     unsigned long long *ck = sc.get<unsigned long long>(S);
     uint32_t *olist = sc.get<uint32_t>(S), *nl = sc.get<uint32_t>(S + 1), *escan = sc.get<uint32_t>(S + 1);
-    uint32_t *posof = sc.get<uint32_t>(N);
+    uint32_t *posof = sc.get<uint32_t>(N), *ctf_of = sc.get<uint32_t>(N);
     uint16_t *nsids = sc.get<uint16_t>(N);
     if (sc.e != cudaSuccess) return cuda_fail(sc.e, "scratch");
     k_cmp_list2<<<grid_for(N, 256), 256, 0, s>>>(N, is2, pos2, xkey, lk, lv);
-    if ((e = radix_sort_u64(lk, lv, lk2, lv2, S, 64, rs_tmp, scan_tmp, s)) != cudaSuccess)
+    if ((e = radix_sort_u64(lk, lv, lk2, lv2, S, 32, rs_tmp, scan_tmp, s)) != cudaSuccess)
         return cuda_fail(e, "x sort");
     /* lv: the x order.  Inside each x part by y (stable), then by part */
     k_cmp_ykeys<<<grid_for(S, 256), 256, 0, s>>>(S, lv, ykey, yk, yv);
-    if ((e = radix_sort_u64(yk, yv, lk2, lv2, S, 64, rs_tmp, scan_tmp, s)) != cudaSuccess)
+    if ((e = radix_sort_u64(yk, yv, lk2, lv2, S, 32, rs_tmp, scan_tmp, s)) != cudaSuccess)
         return cuda_fail(e, "y sort");
     k_cmp_parts<<<grid_for(S, 256), 256, 0, s>>>(S, split, x_part, sn, yv, yk);
     if ((e = radix_sort_u64(yk, yv, lk2, lv2, S, 16, rs_tmp, scan_tmp, s)) != cudaSuccess)
@@ -639,8 +781,13 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
     /* sids: the class (0, 1, 2), then the CTF of every placed position; the
      * placed objects in (CTF, oid) order */
     k_cmp_sids_init<<<grid_for(N, 256), 256, 0, s>>>(N, cls, nsids);
-    if (split) k_cmp_assign<<<grid_for(split, 256), 256, 0, s>>>(split, x_part, y_part, sn, yv, lv, nsids, ck, olist);
-    if ((e = radix_sort_u64(ck, olist, lk2, lv2, split, 42, rs_tmp, scan_tmp, s)) != cudaSuccess)
+    cudaMemsetAsync(ctf_of, 0xff, sizeof(uint32_t) * N, s);
+    if (split) k_cmp_assign<<<grid_for(split, 256), 256, 0, s>>>(split, x_part, y_part, sn, yv, lv, nsids, ctf_of);
+    k_cmp_placed<<<grid_for(N, 256), 256, 0, s>>>(N, ctf_of, is2);
+    scan_u32(is2, pos2, N, scan_tmp, s);
+    k_cmp_plist<<<grid_for(N, 256), 256, 0, s>>>(N, ctf_of, pos2, ck, olist);
+    if ((e = radix_sort_u64(ck, olist, lk2, lv2, split, std::max(1, radix_bits_for(S2 - 1)), rs_tmp, scan_tmp, s)) !=
+        cudaSuccess)
         return cuda_fail(e, "CTF sort");
     cudaMemsetAsync(posof, 0xff, sizeof(uint32_t) * N, s);
     if (split) k_cmp_listn<<<grid_for(split, 256), 256, 0, s>>>(split, olist, nkeys, nl, posof);
@@ -743,27 +890,59 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
     cudaMemsetAsync(nb.bitmaps, 0, (size_t)S2 * kBitBytes, s);
     cudaMemsetAsync(nb.obitmap, 0, kBitBytes, s);
 
-    /* bitmaps and packed keys */
+    /* bitmaps and packed keys: every placed object's records, then object
+     * 0's repeats */
+    std::vector<unsigned long long> h_padk(S2 + 1, 0);
+    for (uint32_t cc = 0; cc < S2; ++cc) h_padk[cc + 1] = h_padk[cc] + h_pad[cc] * n0;
+    unsigned long long *d_padk = sc.get<unsigned long long>(S2 + 1), *obase = sc.get<unsigned long long>(N);
+    if (sc.e != cudaSuccess) {
+        store_block_release(nb);
+        return cuda_fail(sc.e, "scratch");
+    }
+    cudaMemcpyAsync(d_padk, h_padk.data(), sizeof(unsigned long long) * (S2 + 1), cudaMemcpyHostToDevice, s);
+    k_cmp_index<<<grid_for(N, 256), 256, 0, s>>>(N, nsids, nkeys, posof, d_cstart, nb.key_index, d_pad, escan, olist,
+                                                 S2, n0, nb.first, nb.count, obase);
     PackArgs pa;
     pa.ctfs = nb.ctfs;
     pa.key_index = nb.key_index;
     pa.byte_index = nb.byte_index;
     pa.cstart = d_cstart;
     pa.pad = d_pad;
+    pa.padk = d_padk;
     pa.escan = escan;
-    pa.olist = olist;
+    pa.posof = posof;
     pa.rfirst = rfirst;
-    pa.sidx = sval;
-    pa.recs = recs;
+    pa.ctf_of = ctf_of;
+    pa.obase = obase;
+    pa.prec = prec;
     pa.out = nb.keys;
     pa.bits = reinterpret_cast<uint32_t *>(nb.bitmaps);
     pa.counters = d_cnt;
-    pa.kv = KV;
     pa.C = S2;
     pa.n0 = n0;
-    if (KV) k_cmp_pack<<<grid_for(KV, 256), 256, 0, s>>>(pa);
-    k_cmp_index<<<grid_for(N, 256), 256, 0, s>>>(N, nsids, nkeys, posof, d_cstart, nb.key_index, d_pad, escan, olist,
-                                                 S2, n0, nb.first, nb.count);
+    /* the output-order records reuse the parsed records' buffer when they fit */
+    Rec *ordered = KV <= R ? recs : sc.get<Rec>(KV);
+    if (sc.e != cudaSuccess) {
+        store_block_release(nb);
+        return cuda_fail(sc.e, "scratch");
+    }
+    pa.n = R_ctf;
+    if (R_ctf) k_cmp_place<<<grid_for(R_ctf, 256), 256, 0, s>>>(pa, ordered);
+    pa.n = h_padk[S2];
+    if (pa.n) k_cmp_place_pad<<<grid_for(pa.n, 256), 256, 0, s>>>(pa, ordered);
+    /* the pack's chunks: (CTF, first key) for every kPackChunk keys of every CTF */
+    std::vector<uint2> h_chunks;
+    for (uint32_t cc = 0; cc < S2; ++cc)
+        for (uint64_t k = 0; k < h_ki[cc + 1] - h_ki[cc]; k += kPackChunk) h_chunks.push_back(make_uint2(cc, (uint32_t)k));
+    uint2 *d_chunks = sc.get<uint2>(h_chunks.size());
+    if (sc.e != cudaSuccess) {
+        store_block_release(nb);
+        return cuda_fail(sc.e, "scratch");
+    }
+    if (!h_chunks.empty()) {
+        cudaMemcpyAsync(d_chunks, h_chunks.data(), sizeof(uint2) * h_chunks.size(), cudaMemcpyHostToDevice, s);
+        k_cmp_pack<<<(unsigned)h_chunks.size(), 256, 0, s>>>(pa, ordered, d_chunks);
+    }
 
     /* the oversize buffers (merge_dump :1099-1127): the smallest head key is
      * taken each time, ties to the earlier buffer, the extra list last.  For
@@ -775,7 +954,7 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
             const StoreBlock &b = c->ctbs[first + i];
             if (b.o_count) k_cmp_ocheck<<<grid_for(b.o_count, 256), 256, 0, s>>>(b.okeys, b.o_count, d_cnt);
         }
-        if (n_extra > 1) k_cmp_xcheck<<<grid_for(n_extra, 256), 256, 0, s>>>(sval, recs, R_ctf, n_extra, d_cnt);
+        if (n_extra > 1) k_cmp_xcheck<<<grid_for(n_extra, 256), 256, 0, s>>>(prec, R_ctf, n_extra, d_cnt);
         if ((e = cudaMemcpyAsync(hc, d_cnt, sizeof(hc), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
             (e = cudaStreamSynchronize(s)) != cudaSuccess) {
             store_block_release(nb);
@@ -800,7 +979,7 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
         }
         uint64_t at = 0;
         if (extra_first) {
-            k_cmp_ocat<<<grid_for(n_extra, 256), 256, 0, s>>>(nullptr, nullptr, 0, sval, recs, R_ctf, n_extra, olo,
+            k_cmp_ocat<<<grid_for(n_extra, 256), 256, 0, s>>>(nullptr, nullptr, 0, prec, R_ctf, n_extra, olo,
                                                               ohi, obx, 0);
             at = n_extra;
         }
@@ -808,7 +987,7 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
             const StoreBlock &b = c->ctbs[first + i];
             const uint64_t ne = (!extra_first && i + 1 == count) ? n_extra : 0;
             if (b.o_count + ne)
-                k_cmp_ocat<<<grid_for(b.o_count + ne, 256), 256, 0, s>>>(b.okeys, b.oboxes, b.o_count, sval, recs,
+                k_cmp_ocat<<<grid_for(b.o_count + ne, 256), 256, 0, s>>>(b.okeys, b.oboxes, b.o_count, prec,
                                                                          R_ctf, ne, olo, ohi, obx, at);
             at += b.o_count + ne;
         }
