@@ -148,3 +148,38 @@ def test_compaction_domain_errors():
         assert g.store_blocks() == 1
     finally:
         g.close()
+
+
+def test_compaction_past_2_19_objects():
+    """with more than 2^19 objects the flush's packed keys can keep sid bits
+    above the object id (key_bit rounds up past it); the merge reads the id
+    as the reference's readers do, and still equals the oracle bit for bit"""
+    from glint_pipeline_gb300.tracegen import SEED_SCALE, TraceGenerator
+    n, steps = 600_000, 36
+    gen = TraceGenerator(SEED_SCALE + 0x600, n)
+    box, pts = gen.box(), gen.steps(steps)
+    c = Configuration(num_objects=n, num_meeting_buckets=1 << 26, store_keep=8)
+    g = DeviceBench(c, box, pts[0])
+    try:
+        for t in range(steps):
+            g.step(pts[t], t)
+            if t % 12 == 11:
+                g.flush()
+        blocks = [g.block(i) for i in range(g.store_blocks())]
+        # some CTF leaves room above its id field, and a key there carries a sid bit
+        carried = 0
+        for b in blocks:
+            off = 0
+            for m in b["ctfs"]:
+                kb, cnt = int(m["key_bit"]) // 8, int(m["CTF_kv_capacity"])
+                top = 2 * int(m["id_bit"]) + int(m["duration_bit"]) + int(m["end_bit"]) + int(m["mbr_bit"])
+                if int(m["key_bit"]) > top and cnt:
+                    raw = b["keys"][off:off + kb * cnt].reshape(cnt, kb)
+                    hi = np.array([int.from_bytes(r.tobytes(), "little") >> top for r in raw[:200]])
+                    carried += int((hi != 0).sum())
+                off += kb * cnt
+        assert carried > 0
+        box = np.asarray(box, np.float64)
+        compact_and_check(g, n, box, 0, len(blocks), 12)
+    finally:
+        g.close()
