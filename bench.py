@@ -56,7 +56,9 @@ def parse():
     p.add_argument("--objects", type=int, default=10_000_000)
     p.add_argument("--buckets", type=int, default=1 << 30)
     p.add_argument("--mode", default="both", choices=["both", "plain", "tuned"])
-    p.add_argument("--e2e-steps", type=int, default=8)
+    p.add_argument("--e2e-steps", type=int, default=20,
+                   help="host-buffer steps timed through the pipelined API (as many as the timed steps, so the "
+                        "flushes amortise alike)")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
     p.add_argument("--cpu-sample-objects", type=int, default=500_000)
