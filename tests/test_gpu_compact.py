@@ -183,3 +183,33 @@ def test_compaction_past_2_19_objects():
         compact_and_check(g, n, box, 0, len(blocks), 12)
     finally:
         g.close()
+
+
+def test_snapshot_keeps_a_compacted_block(tmp_path):
+    """a snapshot holds kept blocks of any CTF count with their bitmaps,
+    oversize boxes and record times; the resumed context reads them back
+    equal and answers queries alike"""
+    g, n, box = build("dense_20k", 50, (20, 35, 49), dprob=2e-9)
+    h = None
+    try:
+        g.compact(0, 2, 4)                 # blocks: compacted (16 CTFs), flushed (100)
+        path = str(tmp_path / "ctx.snap")
+        g.snapshot(path)
+        h = DeviceBench.resume(path, g.config)
+        assert h.store_blocks() == g.store_blocks() == 2
+        for i in range(2):
+            a, b = g.block(i), h.block(i)
+            check_equal(b, a)
+            assert a["times"] == b["times"] and a["o_times"] == b["o_times"]
+        rng = np.random.default_rng(5)
+        qs = [(rng.choice(n, k, replace=False).astype(np.uint32), hops, 0, 0) for k, hops in [(10, 3), (400, 2)]]
+        x, sx = g.query(qs)
+        y, sy = h.query(qs)
+        assert sx == sy
+        for u, v in zip(x, y):
+            for hu, hv in zip(u, v):
+                np.testing.assert_array_equal(hu, hv)
+    finally:
+        if h is not None:
+            h.close()
+        g.close()
