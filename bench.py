@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--cpu-threads", type=int, default=0, help="0: all host cores")
     p.add_argument("--serve-seconds", type=float, default=6.0)
     p.add_argument("--serve-rate", type=float, default=200.0)
+    p.add_argument("--serve-sweep", default="50,2000",
+                   help="further Poisson rates (req/s) served for --serve-seconds / 2 each; empty: none")
     p.add_argument("--no-serve", action="store_true")
     p.add_argument("--compact-split", type=int, default=56,
                    help="split_num of the compaction leg (the reference tool merges into 56^2 = 3136 CTFs)")
@@ -403,17 +405,12 @@ def run_reference_arm(args, rank, world, pg):
     print(json.dumps(line), flush=True)
 
 
-def serving(args, bench, N, t_hi):
-    """Poisson stream of contact-trace queries against the flushed store,
-    served with continuous batching; plus 2-hop queries from 1000 seeds
-    alone."""
-    import glint_pipeline_gb300 as gp
-    if bench.store_blocks() == 0:
-        return None
-    rng = np.random.default_rng(0x474C494E54000005)
-    srv = gp.Server(bench, max_slots=64)
-    n = max(1, int(args.serve_rate * args.serve_seconds))
-    arrive = np.cumsum(rng.exponential(1.0 / args.serve_rate, n))
+def poisson_stream(srv, rng, N, t_hi, rate, seconds):
+    """queries arriving at `rate` for `seconds`, each submitted when it
+    arrives and retired when its last hop is done: latencies (ms), wall time
+    and objects reached"""
+    n = max(1, int(rate * seconds))
+    arrive = np.cumsum(rng.exponential(1.0 / rate, n))
     qs = []
     for _ in range(n):
         k = int(np.exp(rng.uniform(0, np.log(1000))))
@@ -440,7 +437,24 @@ def serving(args, bench, N, t_hi):
                 lat.append(done_t - inflight.pop(tk))
                 reached += r[2]
     wall = time.perf_counter() - t_start
-    lat = np.array(lat) * 1000.0
+    return np.array(lat) * 1000.0, wall, reached, n
+
+
+def serving(args, bench, N, t_hi):
+    """Poisson stream of contact-trace queries against the flushed store,
+    served with continuous batching, at --serve-rate and the --serve-sweep
+    rates; plus 2-hop queries from 1000 seeds alone."""
+    import glint_pipeline_gb300 as gp
+    if bench.store_blocks() == 0:
+        return None
+    rng = np.random.default_rng(0x474C494E54000005)
+    srv = gp.Server(bench, max_slots=64)
+    lat, wall, reached, n = poisson_stream(srv, rng, N, t_hi, args.serve_rate, args.serve_seconds)
+    sweep = {}
+    for r in [float(x) for x in args.serve_sweep.split(",") if x.strip()]:
+        sl, sw, _, sn = poisson_stream(srv, rng, N, t_hi, r, args.serve_seconds / 2)
+        sweep[f"{r:g}"] = {"queries": sn, "qps": sn / sw, "p50_ms": float(np.percentile(sl, 50)),
+                           "p99_ms": float(np.percentile(sl, 99))}
     # 2-hop queries from 1000 seeds, one at a time
     two = []
     for _ in range(20):
@@ -456,7 +470,7 @@ def serving(args, bench, N, t_hi):
     two = np.array(two)
     return {"queries": n, "rate_req_s": args.serve_rate, "qps": n / wall, "p50_ms": float(np.percentile(lat, 50)),
             "p99_ms": float(np.percentile(lat, 99)), "slots": srv.slots, "store_blocks": bench.store_blocks(),
-            "mean_reached": reached / n,
+            "mean_reached": reached / n, "rates": sweep,
             "mix": "seeds 1-1000 log-uniform, 1-3 hops, window 10-1800 s log-uniform",
             "two_hop_1k_seeds": {"p50_ms": float(np.percentile(two, 50)), "p99_ms": float(np.percentile(two, 99)),
                                  "queries": len(two)}}
