@@ -222,6 +222,7 @@ struct glint_ctx {
     uint8_t *d_ctf_keys = nullptr, *d_bitmaps = nullptr, *d_obitmap = nullptr;
     unsigned long long *d_fmisc = nullptr;
     void *d_rs_tmp = nullptr;
+    uint2 *d_place = nullptr;              /* [N] the key scatter's per-object placement records */
     glint_store_info store;
     std::vector<uint32_t> store_ctf_cap;
     bool store_valid = false;

@@ -239,18 +239,27 @@ __global__ void k_group_starts(uint32_t N, const unsigned long long *__restrict_
     }
 }
 
+/* an object's placement record for the key scatter: its segment start, its
+ * sid and its oversize mark in 8 bytes, so that a key costs one random record
+ * and one random cursor instead of four scattered per-object arrays */
+__global__ void k_obj_place(uint32_t N, const uint32_t *__restrict__ seg_of, const uint16_t *__restrict__ sids,
+                            const uint8_t *__restrict__ over, uint2 *__restrict__ place) {
+    for (uint32_t o = blockIdx.x * blockDim.x + threadIdx.x; o < N; o += gridDim.x * blockDim.x)
+        place[o] = make_uint2(seg_of[o], (uint32_t)sids[o] | ((uint32_t)over[o] << 16));
+}
+
 __global__ void k_key_scatter(const u128 *__restrict__ keys, const float4 *__restrict__ boxes, uint64_t n,
-                              const uint8_t *__restrict__ over, const uint16_t *__restrict__ sids,
-                              const uint32_t *__restrict__ seg_of, uint32_t *__restrict__ cur,
+                              const uint2 *__restrict__ place, uint32_t *__restrict__ cur,
                               u128 *__restrict__ okeys, float4 *__restrict__ oboxes) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
         u128 k = keys[i];
         const uint32_t oid = key_oid(k);
-        const uint32_t pos = seg_of[oid] + atomicAdd(&cur[oid], 1u);
+        const uint32_t slot = atomicAdd(&cur[oid], 1u);
+        const uint2 pl = place[oid];
         /* write_sid_in_key (:798-806) for the CTF part */
-        if (!over[oid]) k = (k & (((u128)1 << kSidShift) - 1)) + ((u128)sids[oid] << kSidShift);
-        okeys[pos] = k;
-        oboxes[pos] = boxes[i];
+        if (!(pl.y >> 16)) k = (k & (((u128)1 << kSidShift) - 1)) + ((u128)(pl.y & 0xffffu) << kSidShift);
+        okeys[pl.x + slot] = k;
+        oboxes[pl.x + slot] = boxes[i];
     }
 }
 
@@ -780,6 +789,7 @@ cudaError_t flush_alloc(glint_ctx *c) {
     FALLOC(c->d_bitmaps, (size_t)C * kBitCount / 8);
     FALLOC(c->d_obitmap, kBitCount / 8);
     FALLOC(c->d_fmisc, 8);
+    FALLOC(c->d_place, N);
 #undef FALLOC
     void *p = nullptr;
     cudaError_t e = cudaMalloc(&p, radix_tmp_bytes(N));
@@ -796,7 +806,7 @@ void flush_free(glint_ctx *c) {
                     c->d_over,
                     c->d_oids, c->d_oids2, c->d_mid, c->d_mid2, c->d_gcount, c->d_gstart, c->d_segof, c->d_segcur,
                     c->d_segbig, c->d_ctf_cap, c->d_ctfs, c->d_ctf_lo, c->d_ctf_n, c->d_ctf_byte, c->d_ctf_keys,
-                    c->d_bitmaps, c->d_obitmap, c->d_fmisc, c->d_rs_tmp};
+                    c->d_bitmaps, c->d_obitmap, c->d_fmisc, c->d_rs_tmp, c->d_place};
     for (void *p : ptrs)
         if (p) cudaFree(p);
 }
@@ -886,10 +896,11 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
     scan_u32(c->d_gcount, c->d_gstart, N, c->d_scan_tmp, s);
     k_group_starts<<<grid_for(N, 256), 256, 0, s>>>(N, gk, gv, c->d_gstart, c->d_segof, d_main);
     cudaMemsetAsync(c->d_segcur, 0, sizeof(uint32_t) * N, s);
+    k_obj_place<<<grid_for(N, 256), 256, 0, s>>>(N, c->d_segof, c->d_sids, c->d_over, c->d_place);
     if (old_kv)
         k_key_scatter<<<grid_for(old_kv, 256, 152u * 16u), 256, 0, s>>>(
-            reinterpret_cast<const u128 *>(c->d_keys), c->d_kvbox, old_kv, c->d_over, c->d_sids, c->d_segof,
-            c->d_segcur, reinterpret_cast<u128 *>(c->d_keys2), c->d_kvbox2);
+            reinterpret_cast<const u128 *>(c->d_keys), c->d_kvbox, old_kv, c->d_place, c->d_segcur,
+            reinterpret_cast<u128 *>(c->d_keys2), c->d_kvbox2);
     std::swap(c->d_keys, c->d_keys2);
     std::swap(c->d_kvbox, c->d_kvbox2);
     u128 *keys = reinterpret_cast<u128 *>(c->d_keys);
