@@ -288,6 +288,11 @@ bool ctf_bits(glint_ctf_meta &c, const glint_box &map, uint32_t num_objects, uin
 cudaError_t radix_sort_u64(unsigned long long *keys, uint32_t *vals, unsigned long long *tmp_k, uint32_t *tmp_v,
                            uint64_t n, int bits, void *rs_tmp, void *scan_tmp, cudaStream_t s);
 size_t radix_tmp_bytes(uint64_t n);
+/* the same, skipping the passes whose digit every key shares (one stream
+ * synchronisation) */
+cudaError_t radix_sort_u64_varying(unsigned long long *keys, uint32_t *vals, unsigned long long *tmp_k,
+                                   uint32_t *tmp_v, uint64_t n, int bits, void *rs_tmp, void *scan_tmp,
+                                   cudaStream_t s);
 int radix_bits_for(unsigned long long max_key);
 void server_free_default(glint_ctx *c);
 void servers_detach(glint_ctx *c);

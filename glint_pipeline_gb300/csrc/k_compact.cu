@@ -769,11 +769,11 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
     uint16_t *nsids = sc.get<uint16_t>(N);
     if (sc.e != cudaSuccess) return cuda_fail(sc.e, "scratch");
     k_cmp_list2<<<grid_for(N, 256), 256, 0, s>>>(N, is2, pos2, xkey, lk, lv);
-    if ((e = radix_sort_u64(lk, lv, lk2, lv2, S, 32, rs_tmp, scan_tmp, s)) != cudaSuccess)
+    if ((e = radix_sort_u64_varying(lk, lv, lk2, lv2, S, 32, rs_tmp, scan_tmp, s)) != cudaSuccess)
         return cuda_fail(e, "x sort");
     /* lv: the x order.  Inside each x part by y (stable), then by part */
     k_cmp_ykeys<<<grid_for(S, 256), 256, 0, s>>>(S, lv, ykey, yk, yv);
-    if ((e = radix_sort_u64(yk, yv, lk2, lv2, S, 32, rs_tmp, scan_tmp, s)) != cudaSuccess)
+    if ((e = radix_sort_u64_varying(yk, yv, lk2, lv2, S, 32, rs_tmp, scan_tmp, s)) != cudaSuccess)
         return cuda_fail(e, "y sort");
     k_cmp_parts<<<grid_for(S, 256), 256, 0, s>>>(S, split, x_part, sn, yv, yk);
     if ((e = radix_sort_u64(yk, yv, lk2, lv2, S, 16, rs_tmp, scan_tmp, s)) != cudaSuccess)

@@ -126,7 +126,27 @@ __global__ void __launch_bounds__(kRsThreads) k_rs_scatter(const unsigned long l
 
 size_t radix_tmp_bytes(uint64_t n) {
     const uint64_t tiles = (n + kRsTile - 1) / kRsTile;
-    return sizeof(uint32_t) * ((size_t)kRsDigits * (tiles ? tiles : 1) + 1) * 2;
+    /* the digit tables, then the keys' OR and AND (radix_sort_u64_varying) */
+    return sizeof(uint32_t) * ((size_t)kRsDigits * (tiles ? tiles : 1) + 1) * 2 + 2 * sizeof(unsigned long long);
+}
+
+/* OR and AND of all keys: the bits that vary */
+__global__ void __launch_bounds__(256) k_rs_bits(const unsigned long long *__restrict__ keys, uint64_t n,
+                                                 unsigned long long *__restrict__ orand) {
+    unsigned long long o = 0, a = ~0ull;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long k = keys[i];
+        o |= k;
+        a &= k;
+    }
+    for (int d = 16; d > 0; d >>= 1) {
+        o |= __shfl_xor_sync(0xffffffffu, o, d);
+        a &= __shfl_xor_sync(0xffffffffu, a, d);
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicOr(&orand[0], o);
+        atomicAnd(&orand[1], a);
+    }
 }
 
 /* Sorts (keys, vals)[0, n) stably by the low `bits` bits of the keys.  tmp_k /
@@ -150,6 +170,47 @@ cudaError_t radix_sort_u64(unsigned long long *keys, uint32_t *vals, unsigned lo
         k_rs_scatter<<<(unsigned)tiles, kRsThreads, 0, s>>>(src_k, src_v, n, shift, off, tiles, dst_k, dst_v);
         std::swap(src_k, dst_k);
         std::swap(src_v, dst_v);
+    }
+    if (passes & 1) {
+        cudaMemcpyAsync(keys, src_k, sizeof(unsigned long long) * n, cudaMemcpyDeviceToDevice, s);
+        cudaMemcpyAsync(vals, src_v, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, s);
+    }
+    return cudaGetLastError();
+}
+
+/* The same sort, without the passes whose 8-bit digit is equal in every key
+ * (such a pass moves nothing): one reduction of the keys' OR and AND, read on
+ * the host, picks the passes.  Synchronises the stream once. */
+cudaError_t radix_sort_u64_varying(unsigned long long *keys, uint32_t *vals, unsigned long long *tmp_k,
+                                   uint32_t *tmp_v, uint64_t n, int bits, void *rs_tmp, void *scan_tmp,
+                                   cudaStream_t s) {
+    if (n < 2 || bits <= 0) return cudaSuccess;
+    const uint64_t tiles = (n + kRsTile - 1) / kRsTile;
+    if (tiles > 0x7fffffffull) return cudaErrorInvalidValue;
+    uint32_t *cnt = static_cast<uint32_t *>(rs_tmp);
+    uint32_t *off = cnt + (size_t)kRsDigits * tiles + 1;
+    unsigned long long *orand =
+        reinterpret_cast<unsigned long long *>(static_cast<uint8_t *>(rs_tmp) + radix_tmp_bytes(n) - 16);
+    cudaMemsetAsync(orand, 0, sizeof(unsigned long long), s);
+    cudaMemsetAsync(orand + 1, 0xff, sizeof(unsigned long long), s);
+    k_rs_bits<<<(unsigned)std::min<uint64_t>((n + 255) / 256, 152 * 8), 256, 0, s>>>(keys, n, orand);
+    unsigned long long h[2];
+    cudaError_t e = cudaMemcpyAsync(h, orand, sizeof(h), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    const unsigned long long varying = h[0] ^ h[1];
+    unsigned long long *src_k = keys, *dst_k = tmp_k;
+    uint32_t *src_v = vals, *dst_v = tmp_v;
+    int passes = 0;
+    for (int shift = 0; shift < bits; shift += 8) {
+        if (!((varying >> shift) & 0xffull)) continue;
+        k_rs_hist<<<(unsigned)tiles, kRsThreads, 0, s>>>(src_k, n, shift, cnt, tiles);
+        e = scan_u32(cnt, off, (size_t)kRsDigits * tiles, scan_tmp, s);
+        if (e != cudaSuccess) return e;
+        k_rs_scatter<<<(unsigned)tiles, kRsThreads, 0, s>>>(src_k, src_v, n, shift, off, tiles, dst_k, dst_v);
+        std::swap(src_k, dst_k);
+        std::swap(src_v, dst_v);
+        ++passes;
     }
     if (passes & 1) {
         cudaMemcpyAsync(keys, src_k, sizeof(unsigned long long) * n, cudaMemcpyDeviceToDevice, s);
