@@ -440,7 +440,7 @@ def poisson_stream(srv, rng, N, t_hi, rate, seconds):
     return np.array(lat) * 1000.0, wall, reached, n
 
 
-def serving(args, bench, N, t_hi):
+def serving(args, bench, N, t_hi, sweep_rates=True):
     """Poisson stream of contact-trace queries against the flushed store,
     served with continuous batching, at --serve-rate and the --serve-sweep
     rates; plus 2-hop queries from 1000 seeds alone."""
@@ -451,7 +451,7 @@ def serving(args, bench, N, t_hi):
     srv = gp.Server(bench, max_slots=64)
     lat, wall, reached, n = poisson_stream(srv, rng, N, t_hi, args.serve_rate, args.serve_seconds)
     sweep = {}
-    for r in [float(x) for x in args.serve_sweep.split(",") if x.strip()]:
+    for r in [float(x) for x in args.serve_sweep.split(",") if x.strip() and sweep_rates]:
         sl, sw, _, sn = poisson_stream(srv, rng, N, t_hi, r, args.serve_seconds / 2)
         sweep[f"{r:g}"] = {"queries": sn, "qps": sn / sw, "p50_ms": float(np.percentile(sl, 50)),
                            "p99_ms": float(np.percentile(sl, 99))}
@@ -862,6 +862,10 @@ def main():
             serve = serving(args, b, N, total)
         if m == modes[0] and not args.no_compact:
             compact = compaction(args, b)
+            if compact and "error" not in compact and not args.no_serve:
+                # the same query stream over the one merged block: a query
+                # scans the same keys, now in one block instead of several
+                compact["serving"] = serving(args, b, N, total, sweep_rates=False)
         b.close()
     rt.cudaFree(dbuf)
     head = forms[modes[0]]
