@@ -50,12 +50,25 @@ struct HopArgs {
     uint32_t A;
 };
 
+/* marks target reached for slot s and appends it to the slot's next list
+ * when it is new; the lanes that call together and append to the same slot
+ * take their places with one atomic (a slot's counter is one address that
+ * every new object of a large frontier would otherwise hit) */
 __device__ inline void visit(const HopArgs &a, uint32_t s, uint32_t next_list, uint32_t target) {
-    if (target >= a.N) return;
-    uint32_t *vis = a.visited + (size_t)s * a.words;
-    const uint32_t bit = 1u << (target & 31);
-    if (atomicOr(&vis[target >> 5], bit) & bit) return;
-    const uint32_t idx = atomicAdd(&a.counts[s], 1u);
+    const unsigned calling = __activemask();
+    bool fresh = false;
+    if (target < a.N) {
+        const uint32_t bit = 1u << (target & 31);
+        fresh = !(atomicOr(&a.visited[(size_t)s * a.words + (target >> 5)], bit) & bit);
+    }
+    const unsigned appending = __ballot_sync(calling, fresh);
+    if (!fresh) return;
+    const unsigned peers = __match_any_sync(appending, s);
+    const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(&a.counts[s], (uint32_t)__popc(peers));
+    base = __shfl_sync(peers, base, leader);
+    const uint32_t idx = base + __popc(peers & ((1u << lane) - 1u));
     if (idx < a.N) a.lists[((size_t)s * 2 + next_list) * a.N + idx] = target;
 }
 
