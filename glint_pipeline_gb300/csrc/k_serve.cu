@@ -125,6 +125,32 @@ __global__ void __launch_bounds__(256) k_serve_hop(HopArgs a) {
     }
 }
 
+/* the new ids of the active slots as (slot rank, id) keys: slot rank r's
+ * count[r] ids start at off[r] */
+__global__ void k_serve_collect(const uint32_t *__restrict__ lists, uint32_t N, const uint32_t *__restrict__ act,
+                                const SlotParam *__restrict__ param, const unsigned long long *__restrict__ off,
+                                uint32_t A, unsigned long long *__restrict__ keys, uint32_t *__restrict__ vals) {
+    const unsigned long long total = off[A];
+    for (unsigned long long i = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; i < total;
+         i += (unsigned long long)gridDim.x * blockDim.x) {
+        uint32_t lo = 0, hi = A; /* off[lo] <= i < off[lo + 1] */
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) / 2;
+            if (off[mid] <= i) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t s = act[lo];
+        const uint32_t id = lists[((size_t)s * 2 + param[s].cur) * N + (i - off[lo])];
+        keys[i] = ((unsigned long long)lo << 32) | id;
+        vals[i] = 0;
+    }
+}
+
+__global__ void k_serve_ids(const unsigned long long *__restrict__ keys, uint64_t n, uint32_t *__restrict__ ids) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x)
+        ids[i] = (uint32_t)keys[i];
+}
+
 /* the seeds of newly admitted slots: visited, and listed as their frontier */
 __global__ void k_serve_seed(const uint32_t *__restrict__ seeds, const unsigned long long *__restrict__ sprefix,
                              const uint32_t *__restrict__ slots, uint32_t n_slots, HopArgs a) {
@@ -189,13 +215,43 @@ struct glint_server {
     std::vector<SlotParam> hparam;
     std::unordered_map<uint64_t, FinishedQuery> done;
     std::vector<uint32_t> buf;
+    /* a hop's new ids of all active slots, sorted by (slot, id) on the device */
+    unsigned long long *rk = nullptr, *rk2 = nullptr, *roff = nullptr;
+    uint32_t *rv = nullptr, *rv2 = nullptr, *rids = nullptr;
+    void *rs_tmp = nullptr, *rscan = nullptr;
+    uint64_t r_cap = 0;
 };
 
 static void server_release(glint_server *v) {
     void *ps[] = {v->visited, v->lists, v->counts, v->active, v->seed_slots, v->param, v->scanned, v->prefix,
-                  v->sprefix, v->seeds, v->blocks};
+                  v->sprefix, v->seeds, v->blocks, v->rk, v->rk2, v->roff, v->rv, v->rv2, v->rids, v->rs_tmp,
+                  v->rscan};
     for (void *p : ps)
         if (p) cudaFree(p);
+}
+
+/* the results' sort buffers for n ids over `act` slots (grown, never shrunk) */
+static cudaError_t server_result_space(glint_server *v, uint64_t n, uint32_t act) {
+    if (n <= v->r_cap && v->roff) return cudaSuccess;
+    const uint64_t cap = std::max<uint64_t>(n, 1u << 20);
+    void *ps[] = {v->rk, v->rk2, v->rv, v->rv2, v->rids, v->rs_tmp, v->rscan};
+    for (void *p : ps)
+        if (p) cudaFree(p);
+    v->rk = v->rk2 = nullptr;
+    v->rv = v->rv2 = v->rids = nullptr;
+    v->rs_tmp = v->rscan = nullptr;
+    v->r_cap = 0;
+    cudaError_t e = cudaMalloc((void **)&v->rk, sizeof(unsigned long long) * cap);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&v->rk2, sizeof(unsigned long long) * cap);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&v->rv, sizeof(uint32_t) * cap);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&v->rv2, sizeof(uint32_t) * cap);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&v->rids, sizeof(uint32_t) * cap);
+    if (e == cudaSuccess) e = cudaMalloc(&v->rs_tmp, radix_tmp_bytes(cap));
+    if (e == cudaSuccess) e = cudaMalloc(&v->rscan, scan_tmp_bytes(256 * ((cap + 1023) / 1024) + 1));
+    if (e == cudaSuccess && !v->roff) e = cudaMalloc((void **)&v->roff, sizeof(unsigned long long) * (v->slots + 1));
+    if (e == cudaSuccess) v->r_cap = cap;
+    (void)act;
+    return e;
 }
 
 extern "C" glint_status glint_server_create(glint_ctx *c, uint32_t max_slots, glint_server **out) {
@@ -388,18 +444,36 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
         std::vector<uint32_t> cnt(v->slots);
         cudaMemcpyAsync(cnt.data(), v->counts, sizeof(uint32_t) * v->slots, cudaMemcpyDeviceToHost, s);
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return server_fail(v, e, "hop");
-        for (uint32_t k : act) {
+        /* the hop's new ids of every active slot, in (slot, id) order: one
+         * sort and one copy for all of them */
+        std::vector<unsigned long long> roff(act.size() + 1, 0);
+        for (size_t i = 0; i < act.size(); ++i) roff[i + 1] = roff[i] + std::min(cnt[act[i]], N);
+        const uint64_t total = roff.back();
+        if (total) {
+            if ((e = server_result_space(v, total, (uint32_t)act.size())) != cudaSuccess)
+                return server_fail(v, e, "results");
+            for (uint32_t k : act) v->hparam[k].cur ^= 1u; /* the lists the hop wrote */
+            cudaMemcpyAsync(v->param, v->hparam.data(), sizeof(SlotParam) * v->slots, cudaMemcpyHostToDevice, s);
+            cudaMemcpyAsync(v->roff, roff.data(), sizeof(unsigned long long) * roff.size(), cudaMemcpyHostToDevice,
+                            s);
+            k_serve_collect<<<grid_for(total, 256), 256, 0, s>>>(v->lists, N, v->active, v->param, v->roff,
+                                                                 (uint32_t)act.size(), v->rk, v->rv);
+            for (uint32_t k : act) v->hparam[k].cur ^= 1u;
+            const int bits = 32 + std::max(1, radix_bits_for(act.size() - 1));
+            if ((e = radix_sort_u64(v->rk, v->rv, v->rk2, v->rv2, total, bits, v->rs_tmp, v->rscan, s)) !=
+                cudaSuccess)
+                return server_fail(v, e, "results sort");
+            k_serve_ids<<<grid_for(total, 256), 256, 0, s>>>(v->rk, total, v->rids);
+            v->buf.resize(total);
+            cudaMemcpyAsync(v->buf.data(), v->rids, sizeof(uint32_t) * total, cudaMemcpyDeviceToHost, s);
+            if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return server_fail(v, e, "results");
+        }
+        for (size_t ai = 0; ai < act.size(); ++ai) {
+            const uint32_t k = act[ai];
             SlotState &st = v->state[k];
             const uint32_t got = std::min(cnt[k], N);
             const uint32_t nl = v->hparam[k].cur ^ 1u;
-            if (got) {
-                v->buf.resize(got);
-                e = cudaMemcpy(v->buf.data(), v->lists + ((size_t)k * 2 + nl) * N, sizeof(uint32_t) * got,
-                               cudaMemcpyDeviceToHost);
-                if (e != cudaSuccess) return server_fail(v, e, "results");
-                std::sort(v->buf.begin(), v->buf.end());
-                st.ids.insert(st.ids.end(), v->buf.begin(), v->buf.end());
-            }
+            if (got) st.ids.insert(st.ids.end(), v->buf.begin() + roff[ai], v->buf.begin() + roff[ai + 1]);
             st.hop_end[st.hop] = st.ids.size();
             ++st.hop;
             st.frontier = got;
