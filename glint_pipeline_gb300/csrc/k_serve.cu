@@ -442,7 +442,9 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
         const unsigned long long items = prefix.back() * nb;
         if (items) k_serve_hop<<<grid_for(items, 256, 152u * 16u), 256, 0, s>>>(a);
         std::vector<uint32_t> cnt(v->slots);
+        std::vector<unsigned long long> scanned(v->slots);
         cudaMemcpyAsync(cnt.data(), v->counts, sizeof(uint32_t) * v->slots, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(scanned.data(), v->scanned, sizeof(unsigned long long) * v->slots, cudaMemcpyDeviceToHost, s);
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return server_fail(v, e, "hop");
         /* the hop's new ids of every active slot, in (slot, id) order: one
          * sort and one copy for all of them */
@@ -480,12 +482,10 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
             v->hparam[k].cur = nl;
             if (st.hop >= st.hops || got == 0) {
                 for (uint32_t h = st.hop; h < kMaxHops; ++h) st.hop_end[h] = st.ids.size();
-                unsigned long long sc = 0;
-                cudaMemcpy(&sc, v->scanned + k, sizeof(sc), cudaMemcpyDeviceToHost);
                 FinishedQuery f;
                 f.ids = std::move(st.ids);
                 std::memcpy(f.hop_end, st.hop_end, sizeof(f.hop_end));
-                f.keys_scanned = sc;
+                f.keys_scanned = scanned[k];
                 v->done[st.ticket] = std::move(f);
                 st = SlotState();
             }
