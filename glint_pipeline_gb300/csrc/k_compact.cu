@@ -119,9 +119,7 @@ __device__ inline u128 load_key(const uint8_t *p, uint32_t kb, const uint8_t *en
         v = ((u128)w1 << 64 | w0) >> sh;
         if (sh) v |= (u128)w[2] << (128 - sh);
     } else {
-        v = 0;
-        for (uint32_t t = 0; t < kb; ++t) v |= (u128)p[t] << (8 * t);
-        return v;
+        return get_key_bytes(p, kb);
     }
     return kb < 16 ? v & (((u128)1 << (8 * kb)) - 1) : v;
 }
@@ -440,7 +438,7 @@ __global__ void __launch_bounds__(256) k_cmp_pack(PackArgs a, const Rec *__restr
             const u128 key = ((u128)r.oid << (m.id_bit + m.duration_bit + m.end_bit + m.mbr_bit)) +
                              ((u128)r.target << (m.duration_bit + m.end_bit + m.mbr_bit)) +
                              ((u128)r.duration << (m.end_bit + m.mbr_bit)) + (end << m.mbr_bit) + vm;
-            for (uint32_t j = 0; j < kb; ++j) st[lane * kb + j] = (uint8_t)(key >> (8 * j));
+            put_key_bytes(st + lane * kb, key, kb);
         }
         __syncwarp();
         /* the warp's keys are one run of bytes: aligned words, edge bytes */

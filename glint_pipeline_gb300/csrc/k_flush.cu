@@ -686,7 +686,7 @@ __global__ void k_ctf_pack(const u128 *__restrict__ keys, const float4 *__restri
         const uint32_t kb = m.key_bit / 8;
         const uint64_t at = t.byte_index[c] + (kid - t.key_index[c]) * kb;
         if (at + kb > out_bytes) continue;
-        for (uint32_t j = 0; j < kb; ++j) out[at + j] = (uint8_t)(temp >> (8 * j));
+        put_key_bytes(out + at, temp, kb);
     }
 }
 

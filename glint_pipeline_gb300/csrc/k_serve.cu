@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "glint_internal.cuh"
+#include "store_codec.cuh"
 
 namespace glint {
 
@@ -110,8 +111,7 @@ __global__ void __launch_bounds__(256) k_serve_hop(HopArgs a) {
         const uint8_t *base = blk.keys + blk.byte_index[c] + (unsigned long long)(first - blk.key_index[c]) * kb;
         for (uint32_t j = 0; j < n; ++j) {
             const uint8_t *p = base + (size_t)j * kb;
-            unsigned __int128 v = 0;
-            for (uint32_t t = 0; t < kb; ++t) v |= (unsigned __int128)p[t] << (8 * t);
+            unsigned __int128 v = get_key_bytes(p, kb);
             v >>= m.mbr_bit;
             const uint32_t end = (uint32_t)(v & ((1ull << m.end_bit) - 1)) + blk.end_time_min;
             v >>= m.end_bit;

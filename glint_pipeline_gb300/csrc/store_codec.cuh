@@ -26,6 +26,29 @@ __device__ inline uint64_t serialize_box(const float4 &b, const glint_ctf_meta &
            (x << m.edge_bit) + y;
 }
 
+/* a packed key's kb little-endian bytes (kb <= 16).  The loops are unrolled
+ * over the 16 possible bytes, so every shift is a constant on a 64-bit half;
+ * a loop over kb with a 128-bit shift by 8 j costs a long shift sequence per
+ * byte. */
+__device__ inline void put_key_bytes(uint8_t *dst, unsigned __int128 key, uint32_t kb) {
+    const uint64_t lo = (uint64_t)key, hi = (uint64_t)(key >> 64);
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+        if ((uint32_t)j < kb) dst[j] = (uint8_t)(j < 8 ? lo >> (8 * j) : hi >> (8 * (j - 8)));
+}
+
+__device__ inline unsigned __int128 get_key_bytes(const uint8_t *src, uint32_t kb) {
+    uint64_t lo = 0, hi = 0;
+#pragma unroll
+    for (int j = 0; j < 16; ++j)
+        if ((uint32_t)j < kb) {
+            const uint64_t b = src[j];
+            if (j < 8) lo |= b << (8 * j);
+            else hi |= b << (8 * (j - 8));
+        }
+    return ((unsigned __int128)hi << 64) | lo;
+}
+
 } // namespace glint
 
 #endif
