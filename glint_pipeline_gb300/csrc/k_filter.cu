@@ -123,22 +123,57 @@ struct FilterArgs {
     DevCounters *cnt;
 };
 
-__global__ void __launch_bounds__(128) k_filter_walk(FilterArgs a, uint32_t *__restrict__ qcount,
-                                                     uint32_t *__restrict__ qtmp) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < a.N; i += gridDim.x * blockDim.x) {
-        const uint32_t pid = a.sorted[i];
-        const uint32_t lv = a.obj_lv[pid];
-        uint32_t kept = 0;
-        if (lv != a.obj_leaf[pid]) {
-            const WalkPoint w = walk_point(a.sxy[i], a.sipos[i], a.sc[i], a.f);
-            uint32_t *row = qtmp + (size_t)pid * kQInline;
-            kept = lookup_walk(a.nodes, a.low, a.ibox, lv, w, a.f, a.ex, a.cnt, [&](uint32_t gid, uint32_t k) {
-                if (k < kQInline) row[k] = gid;
-            });
-            atomicAdd(&a.cnt->border_objects, 1u);
+/* Only border objects (a leaf beside their own in reach) walk the tree:
+ * about half of them at 10M objects.  Each warp reads 32 consecutive ranks
+ * at a time, queues its border objects in shared memory, and walks them 32 at
+ * a time, so that every lane of a walk has an object. */
+constexpr int kWalkWarps = 4;
+
+__global__ void __launch_bounds__(32 * kWalkWarps) k_filter_walk(FilterArgs a, uint32_t *__restrict__ qcount,
+                                                                 uint32_t *__restrict__ qtmp) {
+    __shared__ uint32_t sbuf[kWalkWarps][64];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const uint32_t stride = gridDim.x * kWalkWarps * 32;
+    uint32_t nb = 0, nborder = 0;
+    for (uint32_t base = (blockIdx.x * kWalkWarps + wid) * 32;; base += stride) {
+        const bool more = base < a.N;
+        if (more) {
+            const uint32_t i = base + lane;
+            bool border = false;
+            if (i < a.N) {
+                const uint32_t pid = a.sorted[i];
+                border = a.obj_lv[pid] != a.obj_leaf[pid];
+                if (!border) qcount[pid] = 0;
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, border);
+            if (border) sbuf[wid][nb + __popc(m & ((1u << lane) - 1u))] = i;
+            nb += __popc(m);
+            nborder += __popc(m);
+            __syncwarp();
         }
-        qcount[pid] = kept;
+        if (nb >= 32 || (!more && nb > 0)) {
+            const uint32_t take = nb < 32 ? nb : 32;
+            if ((uint32_t)lane < take) {
+                const uint32_t i = sbuf[wid][lane];
+                const uint32_t pid = a.sorted[i];
+                const WalkPoint w = walk_point(a.sxy[i], a.sipos[i], a.sc[i], a.f);
+                uint32_t *row = qtmp + (size_t)pid * kQInline;
+                qcount[pid] = lookup_walk(a.nodes, a.low, a.ibox, a.obj_lv[pid], w, a.f, a.ex, a.cnt,
+                                          [&](uint32_t gid, uint32_t k) {
+                                              if (k < kQInline) row[k] = gid;
+                                          });
+            }
+            const uint32_t rest = nb - take;
+            __syncwarp();
+            const uint32_t v = (uint32_t)lane < rest ? sbuf[wid][32 + lane] : 0u;
+            __syncwarp();
+            if ((uint32_t)lane < rest) sbuf[wid][lane] = v;
+            __syncwarp();
+            nb = rest;
+        }
+        if (!more && nb == 0) break;
     }
+    if (lane == 0 && nborder) atomicAdd(&a.cnt->border_objects, nborder);
 }
 
 __global__ void __launch_bounds__(128) k_filter_emit(FilterArgs a, const uint32_t *__restrict__ qstart,
@@ -206,7 +241,7 @@ cudaError_t launch_filter(glint_ctx *c) {
     a.f = c->frame;
     a.ex = make_exact(c);
     a.cnt = c->d_cnt;
-    k_filter_walk<<<grid_for(N, 128, 152u * 16u), 128, 0, s>>>(a, c->d_qcount, c->d_qtmp);
+    k_filter_walk<<<grid_for(N, 32 * kWalkWarps, 152u * 16u), 32 * kWalkWarps, 0, s>>>(a, c->d_qcount, c->d_qtmp);
     scan_u32(c->d_qcount, c->d_qstart, N, c->d_scan_tmp, s);
     cudaMemsetAsync(c->d_tcount, 0, sizeof(uint32_t) * (G + 1), s);
     cudaMemsetAsync(c->d_tcursor, 0, sizeof(uint32_t) * G, s);
