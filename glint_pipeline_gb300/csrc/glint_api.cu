@@ -179,7 +179,7 @@ void free_all(glint_ctx *c) {
                     c->d_events, c->d_evpos, c->d_evlist, c->d_evdata, c->d_evlevel, c->d_big, c->d_qcount,
                     c->d_qstart, c->d_qlist, c->d_qtmp, c->d_tcount, c->d_tstart, c->d_tcursor, c->d_tlist, c->d_tab,
                     c->d_stamp, c->d_newline, c->d_new, c->d_rextra, c->d_tile_cnt, c->d_tile_off, c->d_log, c->d_cnt, c->d_coef,
-                    c->d_scan_tmp, c->d_qbits, c->d_qpids, c->d_qout, c->d_qn};
+                    c->d_scan_tmp, c->d_scan_tmp_side, c->d_qbits, c->d_qpids, c->d_qout, c->d_qn};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     flush_free(c);
@@ -198,6 +198,9 @@ void free_all(glint_ctx *c) {
         for (auto &e : c->timers.ev) cudaEventDestroy(e);
         for (auto &e : c->flush_ev) cudaEventDestroy(e);
     }
+    if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+    if (c->join_ev) cudaEventDestroy(c->join_ev);
+    if (c->side) cudaStreamDestroy(c->side);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -321,7 +324,17 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     c->device = (int)cfg.device;
     cudaSetDevice(c->device);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e != cudaSuccess) { glint_status st = cuda_fail(c, e, "stream"); delete c; return st; }
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        glint_status st = cuda_fail(c, e, "stream");
+        if (c->fork_ev) cudaEventDestroy(c->fork_ev);
+        if (c->side) cudaStreamDestroy(c->side);
+        if (c->stream) cudaStreamDestroy(c->stream);
+        delete c;
+        return st;
+    }
 
     /* sizes, tracing/workbench.cpp:36-47 */
     const uint32_t N = cfg.num_objects;
@@ -427,6 +440,9 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
         uint8_t *tmp = nullptr;
         ALLOC(tmp, c->scan_tmp_bytes);
         c->d_scan_tmp = tmp;
+        uint8_t *tmp2 = nullptr;
+        ALLOC(tmp2, c->scan_tmp_bytes);
+        c->d_scan_tmp_side = tmp2;
     }
 #undef ALLOC
     if ((e = flush_alloc(c)) != cudaSuccess) {
@@ -588,10 +604,21 @@ static void launch_step(glint_ctx *c, const double *points, bool host) {
     if (tm) cudaEventRecord(c->timers.ev[4], s);
     launch_insert(c, 0);
     if (tm) cudaEventRecord(c->timers.ev[5], s);
+    /* The schema update reads the leaf counts and rewrites the schema and its
+     * stacks; identify and the key append use the table, the log and the
+     * key buffers.  Neither reads what the other writes, so the update runs
+     * on the side stream while identify streams the table. */
+    const bool schema = c->cfg.dynamic_schema != 0;
+    if (schema) {
+        cudaEventRecord(c->fork_ev, s);
+        cudaStreamWaitEvent(c->side, c->fork_ev, 0);
+        launch_schema_update(c, c->side, c->d_scan_tmp_side);
+        cudaEventRecord(c->join_ev, c->side);
+    }
     launch_identify(c, 0);
     launch_keys(c);
     if (tm) cudaEventRecord(c->timers.ev[6], s);
-    if (c->cfg.dynamic_schema) launch_schema_update(c);
+    if (schema) cudaStreamWaitEvent(s, c->join_ev, 0);
     k_step_tail<<<1, 1, 0, s>>>(c->d_qstart, c->N, c->d_cnt);
     if (tm) cudaEventRecord(c->timers.ev[7], s);
     cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, s);

@@ -140,6 +140,10 @@ struct glint_ctx {
     glint_box mbr;
     int device = 0;
     cudaStream_t stream = nullptr;
+    /* the schema update runs here, beside identify, between two events of
+     * the step stream */
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
     std::string last_error;
 
     uint32_t N = 0, G = 0, S = 0, cap = 0;
@@ -250,6 +254,7 @@ struct glint_ctx {
     glint::DevCounters *h_cnt = nullptr;   /* pinned */
     glint::SinCoef *d_coef = nullptr;
     void *d_scan_tmp = nullptr;
+    void *d_scan_tmp_side = nullptr;       /* the schema update's, as it runs beside identify */
     size_t scan_tmp_bytes = 0;
     double2 *h_stage = nullptr;            /* pinned staging for host points (optional) */
     glint::StepParams *h_params = nullptr; /* pinned: the next step's parameters */
@@ -275,7 +280,7 @@ cudaError_t launch_filter(glint_ctx *c);
 cudaError_t launch_refine(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_insert(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_identify(glint_ctx *c, uint32_t cur_time);
-cudaError_t launch_schema_update(glint_ctx *c);
+cudaError_t launch_schema_update(glint_ctx *c, cudaStream_t s, void *scan_tmp);
 cudaError_t launch_keys(glint_ctx *c);
 cudaError_t flush_alloc(glint_ctx *c);
 void flush_free(glint_ctx *c);

@@ -61,7 +61,10 @@ __global__ void __launch_bounds__(256) k_descend(const double2 *__restrict__ pts
         obj_gid[pid] = gid;
         obj_lv[pid] = lv;
         obj_leaf[pid] = cur;
-        atomicAdd(&grid_count[gid], 1u);
+        /* objects come in the previous step's leaf order, so the lanes of a
+         * warp mostly share a leaf: one atomic per leaf and warp */
+        const unsigned peers = __match_any_sync(__activemask(), gid);
+        if ((threadIdx.x & 31) == __ffs(peers) - 1) atomicAdd(&grid_count[gid], (uint32_t)__popc(peers));
     }
 }
 

@@ -417,8 +417,7 @@ __global__ void __launch_bounds__(256) k_sch_apply_split(DNode *__restrict__ nod
 size_t schema_stack_smem(uint32_t win_cap) { return (size_t)win_cap * sizeof(uint32_t); }
 constexpr uint32_t kWinCap = 40000; /* window entries in shared memory (160 KB) */
 
-cudaError_t launch_schema_update(glint_ctx *c) {
-    cudaStream_t s = c->stream;
+cudaError_t launch_schema_update(glint_ctx *c, cudaStream_t s, void *scan_tmp) {
     const uint32_t S = c->S;
     ExactCtx ex = make_exact(c);
     cudaMemsetAsync(&c->d_cnt->n_cand, 0, sizeof(unsigned int), s);
@@ -429,7 +428,7 @@ cudaError_t launch_schema_update(glint_ctx *c) {
     k_sch_cascade<<<1, 1024, 0, s>>>(c->d_nodes, c->d_split, c->d_evscan, c->d_newgid, c->d_cand,
                                      c->cfg.grid_capacity, c->cfg.schema_update_delay, c->d_cnt);
     k_sch_mark<<<grid_for(S, 256, 152u * 8u), 256, 0, s>>>(c->d_nodes, c->d_split, S, c->d_events, c->d_cnt);
-    scan_u32(c->d_events, c->d_evpos, S, c->d_scan_tmp, s);
+    scan_u32(c->d_events, c->d_evpos, S, scan_tmp, s);
     k_sch_compact<<<grid_for(S, 256, 152u * 8u), 256, 0, s>>>(c->d_events, c->d_evpos, S, c->d_evlist, c->d_cnt);
     k_sch_evdata<<<152, 256, 0, s>>>(c->d_nodes, c->d_split, c->d_newgid, c->d_evlist, c->d_evdata, c->d_cnt);
     k_sch_stacks<<<1, kStackThreads, schema_stack_smem(kWinCap), s>>>(c->d_sstack, c->d_gstack, S, c->G, c->d_evdata,

@@ -163,7 +163,9 @@ typedef struct glint_step_stats {
     uint32_t error_flags;          /* GLINT_EF_* */
     uint32_t launches;             /* kernels the step launched */
     uint64_t meeting_log_size;     /* meetings written to the device log so far */
-    float ms[8];                   /* copy, partition, filter, refine, insert, identify, schema, total */
+    float ms[8];                   /* copy, partition, filter, refine, insert, identify, schema (what is
+                                      left of the schema update after identify, beside which it runs),
+                                      total */
     uint64_t kv_count;             /* keys pending for the next flush (workbench::kv_count) */
     uint32_t flushed;              /* 1: this step ended with an automatic flush */
     float flush_ms;                /* its device time (not included in ms[7]) */
