@@ -324,7 +324,14 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     c->device = (int)cfg.device;
     cudaSetDevice(c->device);
     cudaError_t e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        /* the highest priority: the schema update's one-block stack replay
+         * needs 160 KB of shared memory on one SM, which identify's many
+         * short blocks would otherwise keep taking first */
+        int least = 0, greatest = 0;
+        cudaDeviceGetStreamPriorityRange(&least, &greatest);
+        e = cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, greatest);
+    }
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming);
     if (e != cudaSuccess) {
