@@ -64,6 +64,8 @@ class GoCounts(ctypes.Structure):
         ("n_merges", ctypes.c_uint32),
         ("x_buffer", ctypes.c_double),
         ("y_buffer", ctypes.c_double),
+        ("range_reruns", ctypes.c_uint32),
+        ("pad1", ctypes.c_uint32),
     ]
 
 
@@ -115,6 +117,9 @@ def _load_oracle():
     vp = ctypes.c_void_p
     lib.go_create.restype = vp
     lib.go_create.argtypes = [ctypes.POINTER(GoConfig), vp, vp]
+    lib.go_create_threads.restype = vp
+    lib.go_create_threads.argtypes = [ctypes.POINTER(GoConfig), vp, vp, ctypes.c_uint32]
+    lib.go_set_threads.argtypes = [vp, ctypes.c_uint32]
     lib.go_destroy.argtypes = [vp]
     lib.go_step.argtypes = [vp, vp, ctypes.c_uint32]
     lib.go_get_counts.argtypes = [vp, ctypes.POINTER(GoCounts)]
@@ -171,14 +176,19 @@ def make_config(num_objects, *, grid_capacity=50, schema_update_delay=1, min_mee
 
 
 class Oracle:
-    """Single-threaded CPU restatement of the reference's per-step stages."""
+    """CPU restatement of the reference's per-step stages.  threads > 1 runs
+    the order-free parts on host threads; the results are those of one
+    thread."""
 
-    def __init__(self, cfg: GoConfig, mbr: np.ndarray, first_points: np.ndarray):
+    def __init__(self, cfg: GoConfig, mbr: np.ndarray, first_points: np.ndarray, threads: int = 1):
         self.lib = oracle_lib()
         self.cfg = cfg
         self._mbr = np.ascontiguousarray(mbr, dtype=np.float64)
         pts = np.ascontiguousarray(first_points, dtype=np.float64)
-        self.h = self.lib.go_create(ctypes.byref(cfg), self._mbr.ctypes.data, pts.ctypes.data)
+        self.h = self.lib.go_create_threads(ctypes.byref(cfg), self._mbr.ctypes.data, pts.ctypes.data,
+                                            max(1, int(threads)))
+        if not self.h:
+            raise MemoryError("go_create failed")
 
     def step(self, points: np.ndarray, cur_time: int):
         pts = np.ascontiguousarray(points, dtype=np.float64)

@@ -77,6 +77,8 @@ typedef struct go_counts {
     uint32_t n_merges;            /* schema merges in the last step */
     double x_buffer;
     double y_buffer;
+    uint32_t range_reruns;        /* slot ranges run again for probes crossing range ends (threads > 1) */
+    uint32_t pad1;
 } go_counts;
 
 typedef struct go_ctx go_ctx;
@@ -90,6 +92,10 @@ void go_cantor_inverse(uint64_t z, uint32_t *a, uint32_t *b);
 /* builds the initial schema from the first step's points, as
  * partitioner::build_schema does; mbr4 = low x, low y, high x, high y */
 go_ctx *go_create(const go_config *cfg, const double *mbr4, const double *points_xy);
+/* the same with `threads` host threads for the order-free parts of every
+ * step (go_set_threads); results are identical for every thread count */
+go_ctx *go_create_threads(const go_config *cfg, const double *mbr4, const double *points_xy, uint32_t threads);
+void go_set_threads(go_ctx *c, uint32_t threads);
 void go_destroy(go_ctx *c);
 
 /* one timestep: filter, reachability, update_meetings, update_schema */
