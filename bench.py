@@ -61,8 +61,10 @@ def parse():
                         "flushes amortise alike)")
     p.add_argument("--no-e2e", action="store_true", help="skip the host-buffer pass (profiling runs)")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline (profiling runs)")
-    p.add_argument("--cpu-sample-objects", type=int, default=500_000)
-    p.add_argument("--cpu-sample-steps", type=int, default=3)
+    p.add_argument("--cpu-steps", type=int, default=11,
+                   help="steps the oracle times on the headline workload after --cpu-warmup (its meetings are "
+                        "compared with the GPU's on all of them)")
+    p.add_argument("--cpu-warmup", type=int, default=1)
     p.add_argument("--cpu-threads", type=int, default=0, help="0: all host cores")
     p.add_argument("--serve-seconds", type=float, default=6.0)
     p.add_argument("--serve-rate", type=float, default=200.0)
@@ -121,11 +123,12 @@ class Clocks:
     def __init__(self, device, tag):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{tag}_{os.getpid()}.csv")
+        import tempfile
+        fd, self.path = tempfile.mkstemp(prefix=f"glint_clocks_{tag}_", suffix=".csv")
+        os.close(fd)
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
@@ -149,6 +152,11 @@ class Clocks:
             rows = [[c.strip() for c in r.split(",")] for r in open(self.path).read().strip().splitlines() if r.strip()]
         except Exception:
             return out
+        finally:
+            try:
+                os.unlink(self.path)
+            except OSError:
+                pass
         rows = [r for r in rows if len(r) >= 9]
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         if sm:
@@ -222,9 +230,11 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
     cfg = gp.Configuration(num_objects=N, num_meeting_buckets=args.buckets, device=local, timing=True,
                            precision_mode=1 if mode == "tuned" else 0, auto_flush=True)
     bench = gp.DeviceBench(cfg, box, first)
+    digests = MeetingDigests(N)
     for t in range(W):
         bench.step_device(dbuf.value + t * step_bytes, t)
         bench.sync()
+        digests.add(bench)
     barrier(pg)
     stage_ms = np.zeros(8)
     flush_ms, flushes = 0.0, 0
@@ -237,6 +247,7 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
         for t in range(W, W + K):
             bench.step_device(dbuf.value + t * step_bytes, t)
             st = bench.sync()
+            digests.add(bench)
             stage_ms += np.array(st.ms)
             dev_ms += st.ms[7] + st.flush_ms
             flush_ms += st.flush_ms
@@ -269,6 +280,7 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
     out = {"value": N * K * world / dev_s, "ms_per_step": 1000.0 * dev_s / K,
            "stage_ms": stage, "per_step": per,
            "clocks": clk.summary(), "gpu_launches": launches}
+    out["_digests"], out["_meetings"] = digests.result()
 
     if args.no_e2e:
         out["e2e"] = None
@@ -320,71 +332,161 @@ def run_form(args, mode, N, local, pg, world, box, first, pb, ob, dbuf, step_byt
 
 
 # DRAM bytes per step of each stage's kernels (dram__bytes_read.sum +
-# dram__bytes_write.sum) from the one-pass ncu launch list of the tuned step
-# at 10M objects and 2^30 buckets (profiles/step10m_tuned_dram.md); other
-# workloads report null
+# dram__bytes_write.sum) at 10M objects and 2^30 buckets, the tuned form:
+# from a full capture of each kernel on the 2M-object case scaled by the
+# stage's units, and from the one-pass launch list of the 10M step where
+# noted (profiles/); other workloads report null
 TRAFFIC_10M_2P30 = {"refine": 43.0e9, "identify": 50.6e9, "insert": 26.5e9}
+
+
+def step_bytes_8d(N, per):
+    """Algorithmic bytes of one step by the hot path's byte model:
+    40 B per object (16 B of coordinates read, 4 B leaf key and 4 B id
+    written, 16 B of coordinates re-read in leaf order), 32 B per contact
+    pair (its 16-B table entry read and written) and 48 B per completed
+    meeting (the 16-B record and two 16-B keys); split by stage as the
+    kernels move them."""
+    by = {"partition": 24 * N, "filter": 0, "refine": 16 * N + 32 * per["contacts"], "insert": 0,
+          "identify": 48 * per["meetings"]}
+    return 40 * N + 32 * per["contacts"] + 48 * per["meetings"], by
 
 
 def roofline(form, N, buckets=None, mode=None):
     pk = peaks()
     hbm = pk.get("hbm_gbs")
+    peak = hbm if hbm else 6800.0
     stages = {k: v for k, v in form["stage_ms"].items() if k in ("partition", "filter", "refine", "insert", "identify")}
     top = max(stages, key=stages.get)
     ms = stages[top]
-    by = stage_bytes(top, N, form["per_step"], 1)
+    step_by, by8 = step_bytes_8d(N, form["per_step"])
+    by = by8[top]
     achieved = by / (ms / 1000.0) / 1e9 if ms > 0 else None
-    peak = hbm if hbm else 6800.0
-    traffic = None
-    if N == 10_000_000 and buckets == 1 << 30 and mode == "tuned" and top in TRAFFIC_10M_2P30:
-        traffic = TRAFFIC_10M_2P30[top]
+    measured = N == 10_000_000 and buckets == 1 << 30 and mode == "tuned"
+    traffic = TRAFFIC_10M_2P30.get(top) if measured else None
+    stage_model = {k: stage_bytes(k, N, form["per_step"], 1) for k in stages}
+    ratio = {k: (TRAFFIC_10M_2P30[k] / by8[k] if by8.get(k) else None) for k in TRAFFIC_10M_2P30} if measured else None
     return {"kernel_stage": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak if achieved else None, "traffic": traffic,
-            "traffic_unit": "bytes per step of the stage's kernels (ncu launch list)", "algorithmic_bytes": by,
+            "traffic_unit": "DRAM bytes per step of the stage's kernels", "algorithmic_bytes": by,
+            "model": "40 B/object + 32 B/contact pair + 48 B/meeting; the stage's share",
+            "step_bytes": step_by, "frac_step": step_by / (form["ms_per_step"] / 1000.0) / 1e9 / peak,
+            "traffic_over_algorithmic": ratio,
+            "stage_model_bytes": stage_model,
+            "stage_model": "bytes each stage's kernels must move in this design (table records, lists, "
+                           "stamps); the reference's model counts only the survey's per-unit figures",
             "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "of fallback"}
 
 
-def cpu_baseline(args, steps=None, warm=1):
-    """The reference's CPU stages (the oracle's C restatement, -O2) on the
-    host cores: one independent instance per thread, each on its own sample
-    of the same generator; value = all threads' object-timesteps / wall time.
-    ctypes releases the GIL around every step, so the threads run in
-    parallel."""
-    import threading
+def host_memory_available():
+    """Bytes this process may still allocate: MemAvailable, capped by a
+    cgroup limit where one is set."""
+    avail = None
+    try:
+        for line in open("/proc/meminfo"):
+            if line.startswith("MemAvailable:"):
+                avail = int(line.split()[1]) * 1024
+    except OSError:
+        pass
+    for path, used_path in (("/sys/fs/cgroup/memory.max", "/sys/fs/cgroup/memory.current"),
+                            ("/sys/fs/cgroup/memory/memory.limit_in_bytes",
+                             "/sys/fs/cgroup/memory/memory.usage_in_bytes")):
+        try:
+            lim = open(path).read().strip()
+            if lim != "max" and int(lim) < (1 << 60):
+                room = int(lim) - int(open(used_path).read().strip())
+                avail = room if avail is None else min(avail, room)
+            break
+        except (OSError, ValueError):
+            continue
+    return avail
+
+
+def oracle_bytes(N, B):
+    """host memory the oracle needs at N objects and B buckets: the table,
+    the leaf buffers and their coordinates, the meeting list and the
+    per-step contact lists"""
+    grids = 4 * max(100_000, N // 50)
+    return 32 * B + grids * 100 * 20 + 1100 * N
+
+
+def cpu_baseline(args, N, B, steps, warm, gpu_digests=None):
+    """The reference's CPU stages, as the oracle's C restatement (-O2), on
+    the host cores and on the GPU arm's own workload: the generator at N
+    objects from step 0, B buckets, leaf capacity 50.  The restatement runs
+    the order-free parts on all host threads and gives the results of one
+    thread.  Timed: steps warm .. warm+steps-1 (wall clock around each
+    step).  Every step's meetings are digested as the GPU's are; with
+    gpu_digests given, they are compared step by step."""
+    from glint_pipeline_gb300 import MEETING_DTYPE
     from glint_pipeline_gb300.tracegen import SEED_SCALE, TraceGenerator
-    from oracle.bindings import Oracle, make_config
-    n = args.cpu_sample_objects
-    k = steps if steps is not None else args.cpu_sample_steps
+    from oracle.bindings import Oracle, cantor_inverse, make_config
     threads = args.cpu_threads or os.cpu_count() or 1
-    inst = []
-    for i in range(threads):
-        g = TraceGenerator(SEED_SCALE + 0x100 * i, n)
-        box, pts = g.box(), g.steps(warm + k)
-        o = Oracle(make_config(n, num_meeting_buckets=1 << 23), box, pts[0])
-        for t in range(warm):
-            o.step(pts[t], t)
-        inst.append((o, pts))
-    barrier = threading.Barrier(threads + 1)
-
-    def run(o, pts):
-        barrier.wait()
-        for t in range(warm, warm + k):
-            o.step(pts[t], t)
-
-    ths = [threading.Thread(target=run, args=x) for x in inst]
-    for th in ths:
-        th.start()
-    barrier.wait()
+    need, avail = oracle_bytes(N, B) + 16 * N * (warm + steps), host_memory_available()
+    if avail is not None and need > 0.8 * avail:
+        return {"skipped": f"the oracle needs about {need / 1e9:.0f} GB of host memory; {avail / 1e9:.0f} GB "
+                           f"available"}
+    total = warm + steps
+    g = TraceGenerator(SEED_SCALE, N)
+    box, pts = g.box(), g.steps(total)
+    g.close()
     t0 = time.perf_counter()
-    for th in ths:
-        th.join()
-    dt = time.perf_counter() - t0
-    for o, _ in inst:
+    o = Oracle(make_config(N, num_meeting_buckets=B), box, pts[0], threads=threads)
+    create_s = time.perf_counter() - t0
+    step_s, digests, counts = [], [], []
+    try:
+        for t in range(total):
+            t0 = time.perf_counter()
+            o.step(pts[t], t)
+            dt = time.perf_counter() - t0
+            if t >= warm:
+                step_s.append(dt)
+            mo = o.meetings()
+            rec = np.zeros(mo.shape[0], MEETING_DTYPE)
+            rec["pid1"], rec["pid2"] = cantor_inverse(mo["key"])
+            rec["start"], rec["end"], rec["mbr"] = mo["start"], mo["end"], mo["mbr"]
+            digests.append(meeting_digest(rec))
+            counts.append(int(rec.shape[0]))
+            del mo, rec
+    finally:
         o.close()
-    return {"value": threads * n * k / dt, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{threads} threads x {n} objects of the same generator (one seed per thread), {k} timed "
-                      f"steps after {warm}; the reference's CPU stages as the single-threaded C restatement, one "
-                      f"instance per thread", "ms_per_step": 1000.0 * dt / k}
+    wall = float(sum(step_s))
+    out = {"value": N * steps / wall, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"the GPU arm's workload itself ({N} objects, {B} buckets), steps {warm}..{total - 1} "
+                     f"timed after {warm} untimed; the reference's CPU stages as the C restatement, "
+                     f"{threads} host threads (results identical to one thread)",
+           "ms_per_step": 1000.0 * wall / steps, "steps": steps, "warmup": warm, "create_s": create_s,
+           "cpu_model": cpu_model(), "host_threads_available": os.cpu_count(), "same_config": True}
+    if gpu_digests is not None:
+        n = min(len(gpu_digests), len(digests))
+        diff = [t for t in range(n) if gpu_digests[t] != digests[t]]
+        out["parity"] = {"steps": n, "meetings": int(sum(counts[:n])),
+                         "steps_with_meetings": int(sum(1 for c in counts[:n] if c)), "mismatching_steps": diff,
+                         "compared": "every step's meetings (pid1, pid2, start, end, f32 box bits) in bucket order, "
+                                     "tuned GPU form vs the oracle, SHA-256"}
+    return out
+
+
+def cpu_model():
+    """The host CPU's model name (/proc/cpuinfo; Arm hosts give an implementer
+    and part number instead)."""
+    try:
+        info = open("/proc/cpuinfo").read()
+    except OSError:
+        return None
+    for key in ("model name", "Model", "Hardware"):
+        for line in info.splitlines():
+            if line.startswith(key) and ":" in line:
+                return line.split(":", 1)[1].strip()
+    impl = part = None
+    for line in info.splitlines():
+        if line.startswith("CPU implementer"):
+            impl = line.split(":", 1)[1].strip()
+        if line.startswith("CPU part"):
+            part = line.split(":", 1)[1].strip()
+    parts = {"0xd4f": "Arm Neoverse V2", "0xd40": "Arm Neoverse V1", "0xd0c": "Arm Neoverse N1"}
+    if part:
+        return f"{parts.get(part, 'Arm part ' + part)} (implementer {impl})"
+    return None
 
 
 def run_reference_arm(args, rank, world, pg):
@@ -392,17 +494,28 @@ def run_reference_arm(args, rank, world, pg):
         return
     steps = max(1, min(args.steps, 3))
     warm = max(1, min(args.warmup, 2))
-    cb = cpu_baseline(args, steps=steps, warm=warm)
+    N, B = args.objects, args.buckets
+    cb = cpu_baseline(args, N, B, steps, warm)
+    if "skipped" in cb:
+        print(json.dumps({"impl": "reference", "unavailable": cb["skipped"]}), flush=True)
+        return
     value = cb["value"]
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
             "steps": steps, "warmup": warm, "ms_per_step": cb["ms_per_step"], "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": f"Manhattan-grid generator, {cb['cores']} x {args.cpu_sample_objects}-object "
-                                   f"samples, reach 2 m, min meeting 5, leaf capacity 50",
-                       "objects": args.cpu_sample_objects},
-            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+            "config": workload_config(args, N, "reference CPU stages (C restatement)"),
+            "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample", "cpu_model",
+                                                "same_config")},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def workload_config(args, N, form):
+    return {"workload": f"Manhattan-grid generator (40x40 km, 8 hotspots): {N} objects, FP64 lon/lat, reach 2 m, "
+                        f"min meeting 5, leaf capacity 50, {args.buckets} buckets, flush past 2^26 keys; "
+                        f"headline form '{form}'",
+            "objects": N, "buckets": args.buckets, "form": form,
+            "l2": "inputs larger than L2 (160 MB of points per step, 34 GB table)"}
 
 
 def poisson_stream(srv, rng, N, t_hi, rate, seconds):
@@ -697,18 +810,40 @@ def run_batch(args, local):
 
 
 def meeting_digest(m):
-    """Order-sensitive 64-bit digest of a meeting list (records compared in
-    the order the step reported them)."""
-    w = np.ascontiguousarray(m).view(np.uint64).ravel()
-    h = np.uint64(w.size)
-    chunk = 1 << 24
-    with np.errstate(over="ignore"):
-        for s in range(0, w.size, chunk):
-            x = w[s:s + chunk]
-            k = np.arange(2 * s + 1, 2 * (s + x.size) + 1, 2, dtype=np.uint64) * np.uint64(0x9E3779B97F4A7C15)
-            y = (x ^ (x >> np.uint64(29))) * np.uint64(0xBF58476D1CE4E5B9)
-            h = h + (y * k).sum(dtype=np.uint64)
-    return int(h)
+    """Order-sensitive digest of a meeting list: SHA-256 of its records
+    (pid1, pid2, start, end, f32 box bits) in the order the step reported
+    them."""
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(m).view(np.uint8)).hexdigest()[:24]
+
+
+class MeetingDigests:
+    """Per-step meeting digests taken beside the stepping: each step's
+    meetings are copied into one of two page-locked buffers and hashed on a
+    worker thread while the next step runs (hashlib releases the GIL)."""
+
+    def __init__(self, capacity):
+        import concurrent.futures
+        import glint_pipeline_gb300 as gp
+        self.bufs = [gp.pinned_empty(max(1, capacity), gp.MEETING_DTYPE) for _ in range(2)]
+        self.pool = concurrent.futures.ThreadPoolExecutor(max_workers=2)
+        self.pending = [None, None]
+        self.futs, self.counts = [], []
+
+    def add(self, bench):
+        k = len(self.futs) & 1
+        if self.pending[k] is not None:
+            self.pending[k].result()
+        m = bench.meetings(self.bufs[k])  # a view of bufs[k], or a new array if it holds too few
+        f = self.pool.submit(meeting_digest, m)
+        self.pending[k] = f
+        self.futs.append(f)
+        self.counts.append(int(m.shape[0]))
+
+    def result(self):
+        d = [f.result() for f in self.futs]
+        self.pool.shutdown()
+        return d, self.counts
 
 
 # the 1%-area skew: 5 hotspots whose 2-sigma discs cover 1% of the 40x40 km box
@@ -869,19 +1004,31 @@ def main():
         b.close()
     rt.cudaFree(dbuf)
     head = forms[modes[0]]
-    cpu = cpu_baseline(args) if (rank == 0 and world == 1 and not args.no_cpu) else None
+    parity = {}
+    if len(modes) == 2:
+        dt_, dp_ = forms["tuned"]["_digests"], forms["plain"]["_digests"]
+        ct_, cp_ = forms["tuned"]["_meetings"], forms["plain"]["_meetings"]
+        parity["tuned_vs_plain"] = {
+            "steps": len(dt_), "meetings": int(sum(ct_)), "timed_steps": K,
+            "mismatching_steps": [t for t in range(min(len(dt_), len(dp_))) if dt_[t] != dp_[t] or ct_[t] != cp_[t]],
+            "compared": "every step (warm-up and timed) of the two forms on the same trajectories: meetings "
+                        "(pid1, pid2, start, end, f32 box bits) in bucket order, SHA-256"}
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu:
+        cpu = cpu_baseline(args, N, args.buckets, args.cpu_steps, args.cpu_warmup, head["_digests"])
+        if "parity" in cpu:
+            parity["oracle"] = cpu.pop("parity")
     if compact is not None and rank == 0 and world == 1 and not args.no_cpu:
         compact["sample"] = compaction_sample(args, local)
+    for f in forms.values():
+        f.pop("_digests", None)
+        f.pop("_meetings", None)
     if rank == 0:
         line = {"metric": METRIC, "value": head["value"], "unit": UNIT, "n_gpus": world, "steps": K, "warmup": W,
                 "ms_per_step": head["ms_per_step"], "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f64", "data": "synthetic",
-                "config": {"workload": f"Manhattan-grid generator (40x40 km, 8 hotspots): {N} objects, FP64 "
-                                       f"lon/lat, reach 2 m, min meeting 5, leaf capacity 50, {args.buckets} "
-                                       f"buckets, flush past 2^26 keys; headline form '{modes[0]}'",
-                           "objects": N, "buckets": args.buckets, "form": modes[0],
-                           "l2": "inputs larger than L2 (160 MB of points per step, 34 GB table)"},
-                "roofline": roofline(head, N, args.buckets, modes[0]), "clocks": head["clocks"], "e2e": head["e2e"], "cpu_baseline": cpu,
+                "dtype": "f64", "data": "synthetic", "config": workload_config(args, N, modes[0]),
+                "roofline": roofline(head, N, args.buckets, modes[0]), "clocks": head["clocks"], "e2e": head["e2e"],
+                "cpu_baseline": cpu, "parity": parity,
                 "gpu_launches": head["gpu_launches"], "serving": serve, "compaction": compact,
                 "forms": {m: {k: v for k, v in f.items()} for m, f in forms.items()}}
         print(json.dumps(line), flush=True)

@@ -261,7 +261,8 @@ uint32_t *g_na_ptr[kNaMaxDevices];
 cudaError_t g_na_status[kNaMaxDevices];
 bool g_na_done[kNaMaxDevices];
 
-/* exclusive scan of n (<= kNaMaxTiles + 1) values by one block, no scratch */
+/* exclusive scan of n (<= kNaMaxTiles) values by one block, no scratch;
+ * out[n] receives the total, so out has n + 1 words and in only n are read */
 __global__ void __launch_bounds__(1024) k_scan_one_block(const uint32_t *__restrict__ in, uint32_t *__restrict__ out,
                                                          uint64_t n) {
     __shared__ uint32_t ws[32];
@@ -294,18 +295,19 @@ __global__ void __launch_bounds__(1024) k_scan_one_block(const uint32_t *__restr
         if (threadIdx.x == 0) carry += ws[31];
         __syncthreads();
     }
+    if (threadIdx.x == 0) out[n] = carry;
 }
 
-/* looks up the scratch address on the current device, once per device */
+/* looks up the scratch address on the current device; run by every
+ * glint_create, so a context created after a device reset sees the array's
+ * address in the device's new CUDA context */
 cudaError_t noalloc_setup(int device) {
     if (device < 0 || device >= kNaMaxDevices) return cudaErrorInvalidDevice;
     std::lock_guard<std::mutex> lock(g_na_mutex);
-    if (!g_na_done[device]) {
-        void *p = nullptr;
-        g_na_status[device] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        g_na_ptr[device] = g_na_status[device] == cudaSuccess ? static_cast<uint32_t *>(p) : nullptr;
-        g_na_done[device] = true;
-    }
+    void *p = nullptr;
+    g_na_status[device] = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    g_na_ptr[device] = g_na_status[device] == cudaSuccess ? static_cast<uint32_t *>(p) : nullptr;
+    g_na_done[device] = true;
     return g_na_status[device];
 }
 
@@ -341,7 +343,7 @@ extern "C" glint_status glint_active_search_noalloc(glint_ctx *c, const uint32_t
     uint32_t *tile_cnt = base + kNaBitsWords;
     uint32_t *tile_off = tile_cnt + kNaTileWords;
     auto scan = [](const uint32_t *in, uint32_t *o, uint64_t m, cudaStream_t s) {
-        k_scan_one_block<<<1, 1024, 0, s>>>(in, o, m + 1);
+        k_scan_one_block<<<1, 1024, 0, s>>>(in, o, m);
         return cudaGetLastError();
     };
     static_assert(sizeof(uint64_t) == sizeof(unsigned long long), "u64");

@@ -522,8 +522,9 @@ glint_status glint_active_search(glint_ctx *ctx, const uint32_t *pids, uint32_t 
  * glint_active_search are written to d_out.  Enqueued on the context's stream
  * (glint_stream); returns without waiting.
  * Scratch: one fixed array of the library per device (2 MB id bitmap +
- * 1 MB of tile counters), whose address is looked up once per device inside
- * glint_create with that device current; the call itself performs no
+ * 1 MB of tile counters), whose address is looked up inside every
+ * glint_create with that device current (so a context created after a
+ * device reset uses the new address); the call itself performs no
  * allocation.  The bitmap is cleared by each call; nothing else needs to
  * start at zero.  Limits: contexts of at most 2^24 objects and 2^30 buckets
  * (GLINT_ERR_UNSUPPORTED otherwise).  Calls that overlap in time on the same

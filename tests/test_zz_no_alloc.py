@@ -3,8 +3,11 @@
 The allocation-free entry point takes device arrays and keeps its scratch in a
 fixed device array of the library.  Two calls in a row (with different id
 lists, so the second depends on the first having cleared its bitmap) must
-return exactly what the allocating entry point returns.  This file is named
-to be collected last, after every other GPU test has used the library.
+return exactly what the allocating entry point returns, also when both are
+enqueued on the stream with no host synchronisation between them, and a
+call whose capacity is too small must report the full count, write only cap
+records and leave the rest of the caller's buffer untouched.  This file is
+named to be collected last, after every other GPU test has used the library.
 """
 import ctypes
 import glob
@@ -89,6 +92,44 @@ def test_noalloc_search_matches_allocating_search():
             got = d_out.download(np.zeros(cap, SEARCH_DTYPE))[:n]
             assert n == len(want)
             assert got.tobytes() == want.tobytes()
+        # truncation: the count is the full count, only cap records are
+        # written, the sentinel bytes after them stay as they were
+        pids = lists[0]
+        want = g.active_search(pids)
+        small = len(want) // 2
+        d_pids.upload(pids)
+        d_out.fill(0xAB)
+        d_n.fill(0)
+        st = lib.glint_active_search_noalloc(g.h, ctypes.c_void_p(d_pids.ptr), len(pids),
+                                             ctypes.c_void_p(d_out.ptr), small, ctypes.c_void_p(d_n.ptr))
+        assert st == 0, g.last_error()
+        assert rt.cudaStreamSynchronize(ctypes.c_void_p(g.stream)) == 0
+        assert int(d_n.download(np.zeros(1, np.uint64))[0]) == len(want)
+        raw = d_out.download(np.zeros(32 * cap, np.uint8))
+        assert raw[:32 * small].tobytes() == want[:small].tobytes()
+        assert np.all(raw[32 * small:] == 0xAB)
+        # two calls enqueued back to back on the context's stream, one host
+        # synchronisation after both
+        outs = [_Dev(rt, 32 * cap), _Dev(rt, 32 * cap)]
+        ins = [_Dev(rt, 4 * len(x)) for x in lists]
+        ns = [_Dev(rt, 8), _Dev(rt, 8)]
+        try:
+            for k, pids in enumerate(lists):
+                ins[k].upload(pids)
+                ns[k].fill(0)
+            for k, pids in enumerate(lists):
+                st = lib.glint_active_search_noalloc(g.h, ctypes.c_void_p(ins[k].ptr), len(pids),
+                                                     ctypes.c_void_p(outs[k].ptr), cap, ctypes.c_void_p(ns[k].ptr))
+                assert st == 0, g.last_error()
+            assert rt.cudaStreamSynchronize(ctypes.c_void_p(g.stream)) == 0
+            for k, pids in enumerate(lists):
+                want = g.active_search(pids)
+                n = int(ns[k].download(np.zeros(1, np.uint64))[0])
+                assert n == len(want)
+                assert outs[k].download(np.zeros(cap, SEARCH_DTYPE))[:n].tobytes() == want.tobytes()
+        finally:
+            for d in outs + ins + ns:
+                d.free()
     finally:
         d_pids.free()
         d_out.free()
