@@ -32,7 +32,6 @@ cudaError_t noalloc_setup(int device);
 inline uint64_t stamp_bytes(uint64_t B) { return identify_tiles(B) * 8192 + 64; }
 /* the new-line bitmap: one bit per 4 slots over the same tiles */
 inline uint64_t newline_words(uint64_t B) { return identify_tiles(B) * (8192 / 128); }
-inline uint64_t touch_words(uint64_t B) { return identify_tiles(B) * (8192 / 32); }
 } // namespace glint
 
 using namespace glint;
@@ -179,7 +178,7 @@ void free_all(glint_ctx *c) {
                     c->d_nodes, c->d_low, c->d_sstack, c->d_gstack, c->d_split, c->d_evscan, c->d_cand, c->d_newgid,
                     c->d_events, c->d_evpos, c->d_evlist, c->d_evdata, c->d_evlevel, c->d_big, c->d_qcount,
                     c->d_qstart, c->d_qlist, c->d_qtmp, c->d_tcount, c->d_tstart, c->d_tcursor, c->d_tlist, c->d_tab,
-                    c->d_stamp, c->d_newline, c->d_touch, c->d_new, c->d_rextra, c->d_tile_cnt, c->d_tile_off, c->d_log, c->d_cnt, c->d_coef,
+                    c->d_stamp, c->d_newline, c->d_new, c->d_rextra, c->d_tile_cnt, c->d_tile_off, c->d_log, c->d_cnt, c->d_coef,
                     c->d_scan_tmp, c->d_scan_tmp_side, c->d_qbits, c->d_qpids, c->d_qout, c->d_qn};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -435,7 +434,6 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     ALLOC(c->d_tab, c->B);
     ALLOC(c->d_stamp, stamp_bytes(c->B));
     ALLOC(c->d_newline, newline_words(c->B));
-    ALLOC(c->d_touch, touch_words(c->B));
     ALLOC(c->d_new, c->new_cap);
     /* each extra refine item is a further kCrossChunk checks of one leaf */
     c->rextra_cap = c->check_cap / kCrossChunk + 1;
@@ -545,7 +543,6 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     k_fill_empty<<<grid_for(c->B, 256, 152u * 16u), 256, 0, c->stream>>>(c->d_tab, c->B);
     cudaMemsetAsync(c->d_stamp, 0, stamp_bytes(c->B), c->stream);
     cudaMemsetAsync(c->d_newline, 0, sizeof(uint32_t) * newline_words(c->B), c->stream);
-    cudaMemsetAsync(c->d_touch, 0, sizeof(uint32_t) * touch_words(c->B), c->stream);
     cudaMemsetAsync(c->d_grid_count, 0, sizeof(uint32_t) * ((size_t)G + 1), c->stream);
     k_iota<<<grid_for(N, 256, 152u * 8u), 256, 0, c->stream>>>(c->d_order, N);
     /* scratch address of glint_active_search_noalloc, once per device, with

@@ -199,7 +199,6 @@ struct glint_ctx {
     glint::TRec *d_tab = nullptr;
     uint8_t *d_stamp = nullptr;
     uint32_t *d_newline = nullptr;   /* one bit per 4 slots filled this step */
-    uint32_t *d_touch = nullptr;     /* one bit per bucket whose pair was touched this step */
     glint::NewEntry *d_new = nullptr;
     uint2 *d_rextra = nullptr;             /* refine work items (leaf, chunk of cross checks) */
     uint64_t rextra_cap = 0;

@@ -8,12 +8,10 @@
  * min_meet_time + 1.  With one thread the reports come out in bucket order
  * (batch_meet, tracing/meeting.cpp:11-24).
  *
- * Device form: a stamp byte per bucket says empty or committed, a bit per
- * bucket says that refine touched its entry this step, and a bit per 128-byte
- * line of the table says that the insert placed a pair in it this step.  The
- * scan reads one byte and one bit per bucket, and the 32-byte records only of
- * committed entries not touched (the ones that expire) and of lines that
- * received a pair; the entries that stay active are counted from the bits.  Pass 1 (32 consecutive buckets
+ * Device form: a stamp byte per bucket says empty or committed, and a bit per
+ * 128-byte line of the table says that the insert placed a pair in it this
+ * step, so the scan reads one byte per bucket and the 32-byte records only of
+ * committed entries and of lines that received a pair.  Pass 1 (32 consecutive buckets
  * per warp and round) finalises entries inserted this step, removes expired
  * entries that are too short, marks the ones to report and counts them per
  * 8192-bucket tile; an exclusive scan gives every tile its offset; pass 2
@@ -38,7 +36,6 @@ constexpr int kIdIlp = 4;
 
 __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict__ stamp,
                                                              uint32_t *__restrict__ newline,
-                                                             uint32_t *__restrict__ touch,
                                                              TRec *__restrict__ tab, uint64_t B, uint32_t min_plus1,
                                                              uint32_t *__restrict__ tile_cnt,
                                                              const float2 *__restrict__ fpos, uint32_t N,
@@ -46,7 +43,6 @@ __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict
     __shared__ uint32_t red[3][kIdThreads / 32];
     __shared__ __align__(16) uint8_t sst[kIdThreads / 32][kIdWarpSpan];
     __shared__ uint32_t snl[kIdThreads / 32][kIdWarpSpan / 128];
-    __shared__ uint32_t stw[kIdThreads / 32][kIdWarpSpan / 32];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const uint64_t wbase = (uint64_t)blockIdx.x * kIdTile + (uint64_t)wid * kIdWarpSpan;
     const uint32_t cur_time = cnt->step_time, st_now = cnt->step_tag;
@@ -60,10 +56,6 @@ __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict
         snl[wid][lane] = newline[(wbase >> 7) + lane];
         newline[(wbase >> 7) + lane] = 0;
     }
-    /* the warp's touch bits: word r covers round r, bit l lane l; cleared
-     * for the next step */
-    stw[wid][lane] = touch[(wbase >> 5) + lane];
-    touch[(wbase >> 5) + lane] = 0;
     __syncwarp();
     uint32_t emit = 0, taken = 0, active = 0;
     for (uint32_t r0 = 0; r0 < kIdWarpSpan / 32; r0 += kIdIlp) {
@@ -74,16 +66,7 @@ __global__ void __launch_bounds__(kIdThreads) k_expire_count(uint8_t *__restrict
         for (int u = 0; u < kIdIlp; ++u) {
             const uint32_t off = (r0 + u) * 32 + lane;
             sv[u] = wbase + off < B ? sst[wid][off] : kStampEmpty;
-            if (sv[u] != kStampEmpty) {
-                /* a committed entry: active when touched, else its record decides */
-                need[u] = !((stw[wid][r0 + u] >> lane) & 1u);
-                if (!need[u]) {
-                    ++taken;
-                    ++active;
-                }
-            } else {
-                need[u] = wbase + off < B && ((snl[wid][off >> 7] >> ((off >> 2) & 31)) & 1u);
-            }
+            need[u] = sv[u] != kStampEmpty || (wbase + off < B && ((snl[wid][off >> 7] >> ((off >> 2) & 31)) & 1u));
             if (need[u]) rec[u] = *reinterpret_cast<const ulonglong2 *>(&tab[wbase + off]);
         }
 #pragma unroll
@@ -223,8 +206,7 @@ cudaError_t launch_identify(glint_ctx *c, uint32_t cur_time) {
     cudaStream_t s = c->stream;
     const uint64_t tiles = identify_tiles(c->B);
     const uint32_t min_plus1 = c->cfg.min_meet_time + 1;
-    k_expire_count<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_newline, c->d_touch, c->d_tab, c->B,
-                                                          min_plus1,
+    k_expire_count<<<(unsigned)tiles, kIdThreads, 0, s>>>(c->d_stamp, c->d_newline, c->d_tab, c->B, min_plus1,
                                                           c->d_tile_cnt,
                                                           c->d_fpos, c->N, c->d_cnt);
     scan_u32(c->d_tile_cnt, c->d_tile_off, tiles, c->d_scan_tmp, s);

@@ -185,7 +185,6 @@ RefineArgs refine_args(glint_ctx *c) {
     a.extra = c->d_rextra;
     a.tab = c->d_tab;
     a.stamp = c->d_stamp;
-    a.touch = c->d_touch;
     a.newlist = c->d_new;
     a.B = c->B;
     a.Bm = c->Bm;
@@ -249,7 +248,7 @@ __device__ inline void touch_box(TRec &r, const float2 &A, const float2 &Bp) {
 }
 
 __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ list, TRec *tab, uint32_t *newline,
-                                                uint32_t *touch, uint64_t B, uint64_t Bm, uint64_t new_cap,
+                                                uint64_t B, uint64_t Bm, uint64_t new_cap,
                                                 const float2 *__restrict__ fpos, uint32_t N,
                                                 DevCounters *cnt) {
     const unsigned long long n0 = cnt->new_keys;
@@ -287,7 +286,6 @@ __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ lis
                     const uint32_t pa = pair_a(plain), pb = pair_b(plain);
                     if (pa < N && pb < N) touch_box(tab[slot], fpos[pa], fpos[pb]);
                     rec_set_tag(tab[slot], st);
-                    atomicOr(&touch[slot >> 5], 1u << (slot & 31));
                     done = true;
                     break;
                 }
@@ -315,7 +313,7 @@ __global__ void __launch_bounds__(256) k_insert(const NewEntry *__restrict__ lis
 
 cudaError_t launch_insert(glint_ctx *c, uint32_t cur_time) {
     (void)cur_time;
-    k_insert<<<152 * 8, 256, 0, c->stream>>>(c->d_new, c->d_tab, c->d_newline, c->d_touch, c->B, c->Bm, c->new_cap, c->d_fpos, c->N,
+    k_insert<<<152 * 8, 256, 0, c->stream>>>(c->d_new, c->d_tab, c->d_newline, c->B, c->Bm, c->new_cap, c->d_fpos, c->N,
                                              c->d_cnt);
     return cudaGetLastError();
 }

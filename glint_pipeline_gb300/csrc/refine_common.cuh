@@ -39,7 +39,6 @@ struct RefineArgs {
     const uint2 *extra;        /* (leaf, chunk) items beyond each leaf's first chunk */
     TRec *tab;
     uint8_t *stamp;
-    uint32_t *touch;           /* bit per bucket touched this step, read and cleared by identify */
     NewEntry *newlist;
     uint64_t B, Bm, new_cap;
     uint32_t cap;
@@ -50,9 +49,7 @@ struct RefineArgs {
 
 /* The table as it stood at the start of the step: keys do not change while
  * the refine kernels run.  Found -> touch the entry (tag, f32 box; each pair
- * has at most one event per step, so the box needs no atomics) and set the
- * bucket's bit in the touch bitmap, which lets identify skip the records of
- * entries that stay active.  Not found
+ * has at most one event per step, so the box needs no atomics).  Not found
  * before an empty slot -> the pair is new this step.  The walk starts at the
  * home slot, whose key word and box the caller has already loaded. */
 __device__ inline bool table_touch_from(const RefineArgs &a, const QEntry &q, uint64_t slot, unsigned long long w0,
@@ -69,7 +66,6 @@ __device__ inline bool table_touch_from(const RefineArgs &a, const QEntry &q, ui
                 *reinterpret_cast<uint4 *>(a.tab[slot].mbr) = m;
             }
             rec_set_tag(a.tab[slot], tag);
-            atomicOr(&a.touch[slot >> 5], 1u << (slot & 31));
             return false;
         }
         if (w0 == kEmptyW0) return true;
