@@ -23,6 +23,32 @@ def build_oracle() -> str:
     return ORACLE_SO
 
 
+REF_GPU_SO = os.path.join(HERE, "_ref", "libglintrefgpu.so")
+REF_CUBIN = os.path.join(HERE, "_ref", "geometry.cubin")
+REF_LAYOUT = os.path.join(HERE, "_ref", "ref_gpu_layout.h")
+
+
+def build_ref_gpu() -> str | None:
+    """Builds the driver that runs the reference's own GPU kernels
+    (ref_gpu_driver.cpp) where build_ref.sh has left their cubin and layout
+    header; returns None where they are absent."""
+    if not (os.path.exists(REF_CUBIN) and os.path.exists(REF_LAYOUT)):
+        return None
+    src = os.path.join(HERE, "ref_gpu_driver.cpp")
+    if os.path.exists(REF_GPU_SO) and os.path.getmtime(REF_GPU_SO) >= max(
+            os.path.getmtime(src), os.path.getmtime(REF_LAYOUT), os.path.getmtime(ORACLE_SO)):
+        return REF_GPU_SO
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    subprocess.run(["g++", "-std=c++17", "-O2", "-fPIC", "-shared", f"-I{HERE}", f"-I{cuda}/include", src,
+                    "-o", REF_GPU_SO, f"-L{cuda}/lib64/stubs", f"-L{cuda}/lib64", "-lcuda", f"-L{HERE}", "-loracle",
+                    "-Wl,-rpath," + HERE], check=True)
+    return REF_GPU_SO
+
+
+def ref_gpu_available() -> bool:
+    return os.path.exists(REF_CUBIN) and os.path.exists(REF_LAYOUT)
+
+
 def build_ref() -> str | None:
     """Builds the reference's own sources when they are present (this
     container); returns None elsewhere."""
@@ -532,3 +558,102 @@ def cantor_inverse(keys: np.ndarray):
     b = (z - t).astype(np.uint64)
     a = (w - b).astype(np.uint64)
     return a.astype(np.uint32), b.astype(np.uint32)
+
+
+class RgConfig(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_uint32), ("num_objects", ctypes.c_uint32), ("CTF_count", ctypes.c_uint32),
+                ("split_num", ctypes.c_uint32), ("min_meet_time", ctypes.c_uint32),
+                ("max_meet_time", ctypes.c_uint32), ("kv_capacity", ctypes.c_uint64), ("dProbFalse", ctypes.c_double),
+                ("mbr", ctypes.c_double * 4)]
+
+
+class RgFlushInfo(ctypes.Structure):
+    _fields_ = [("kv_count", ctypes.c_uint64), ("key_bytes", ctypes.c_uint64), ("oversize_kv_count", ctypes.c_uint32),
+                ("oversize_start_time_min", ctypes.c_uint32), ("oversize_start_time_max", ctypes.c_uint32),
+                ("oversize_end_time_min", ctypes.c_uint32), ("oversize_end_time_max", ctypes.c_uint32),
+                ("sid_count", ctypes.c_uint32), ("oversize_oid_count", ctypes.c_uint32), ("pad", ctypes.c_uint32),
+                ("bits_in_slack", ctypes.c_uint64)]
+
+
+class RefGpu:
+    """The reference's own GPU kernels (cuda/geometry.cu, compiled unmodified
+    into oracle/_ref/geometry.cubin) driven as process_with_gpu drives them:
+    key generation and the active multi-search by cuda_identify_meetings,
+    and the flush into the key-value + bitmap store.  Needs a GPU."""
+
+    def __init__(self, num_objects, mbr, *, CTF_count=100, split_num=10, min_meet_time=5, max_meet_time=4096,
+                 kv_capacity=1 << 22, dProbFalse=100.0, device=0):
+        build_oracle()
+        so = build_ref_gpu()
+        if so is None:
+            raise RuntimeError("the reference's GPU kernels are not built here (oracle/build_ref.sh)")
+        self.lib = lib = ctypes.CDLL(so)
+        vp = ctypes.c_void_p
+        lib.rg_open.argtypes = [ctypes.c_char_p, ctypes.POINTER(RgConfig), ctypes.POINTER(vp)]
+        lib.rg_error.restype = ctypes.c_char_p
+        lib.rg_error.argtypes = [vp]
+        lib.rg_identify.argtypes = [vp, vp, ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, vp, ctypes.c_uint32,
+                                    vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)]
+        lib.rg_pending.argtypes = [vp, ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint32),
+                                   ctypes.POINTER(ctypes.c_uint32)]
+        lib.rg_flush.argtypes = [vp, ctypes.c_uint32, ctypes.POINTER(RgFlushInfo)]
+        lib.rg_result.argtypes = [vp] * 9
+        lib.rg_close.argtypes = [vp]
+        self.n, self.C = int(num_objects), int(CTF_count)
+        cfg = RgConfig(device, self.n, self.C, split_num, min_meet_time, max_meet_time, kv_capacity, dProbFalse,
+                       (ctypes.c_double * 4)(*[float(v) for v in mbr]))
+        self.h = vp()
+        rc = lib.rg_open(REF_CUBIN.encode(), ctypes.byref(cfg), ctypes.byref(self.h))
+        if rc != 0:
+            msg = lib.rg_error(self.h).decode()
+            self.close()
+            raise RuntimeError(f"rg_open: {msg}")
+
+    def _check(self, rc, what):
+        if rc != 0:
+            raise RuntimeError(f"{what} ({rc}): {self.lib.rg_error(self.h).decode()}")
+
+    def identify(self, meetings, cur_time, end_time_min, pids=None):
+        """meetings: MEETING_DTYPE records (Cantor key, start, end, f32 box),
+        the layout of meeting_unit; pids: the multi-search list, or None.
+        Returns the multi-search's records (in the reference's atomic
+        order)."""
+        m = np.ascontiguousarray(meetings, dtype=MEETING_DTYPE)
+        p = np.ascontiguousarray(pids if pids is not None else np.zeros(0), dtype=np.uint32)
+        found = ctypes.c_uint64()
+        cap = 2 * max(1, m.shape[0]) * max(1, int(np.bincount(p).max()) if p.size else 1)
+        out = np.zeros(cap if p.size else 1, SEARCH_DTYPE)
+        rc = self.lib.rg_identify(self.h, m.ctypes.data if m.size else None, m.shape[0], int(cur_time),
+                                  int(end_time_min), p.ctypes.data if p.size else None, p.shape[0], out.ctypes.data,
+                                  out.shape[0], ctypes.byref(found))
+        self._check(rc, "rg_identify")
+        return out[: int(found.value)]
+
+    def pending(self):
+        kv, sc, oc = ctypes.c_uint64(), ctypes.c_uint32(), ctypes.c_uint32()
+        self._check(self.lib.rg_pending(self.h, ctypes.byref(kv), ctypes.byref(sc), ctypes.byref(oc)), "rg_pending")
+        return int(kv.value), int(sc.value), int(oc.value)
+
+    def flush(self, cur_time):
+        info = RgFlushInfo()
+        self._check(self.lib.rg_flush(self.h, int(cur_time), ctypes.byref(info)), "rg_flush")
+        r = {"info": info, "keys": np.zeros(int(info.key_bytes), np.uint8), "sids": np.zeros(self.n, np.uint16),
+             "ctf_capacity": np.zeros(self.C, np.uint32), "ctfs": np.zeros(self.C, CTF_META_DTYPE),
+             "bitmaps": np.zeros(self.C * BIT_BYTES, np.uint8),
+             "o_keys": np.zeros(int(info.oversize_kv_count) * 16, np.uint8),
+             "o_boxes": np.zeros((int(info.oversize_kv_count), 4), np.float32),
+             "o_bitmap": np.zeros(BIT_BYTES, np.uint8)}
+        self.lib.rg_result(self.h, *[r[k].ctypes.data for k in ("keys", "sids", "ctf_capacity", "ctfs", "bitmaps",
+                                                               "o_keys", "o_boxes", "o_bitmap")])
+        return r
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.lib.rg_close(self.h)
+            self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -33,4 +33,20 @@ $CXX $FLAGS -Dmain=glint_ref_compaction_tool_main -c "$SRC/tools/compaction.cpp"
 $CXX $FLAGS -c "$HERE/ref_driver.cpp" -o "$OUT/ref_driver.o" &
 wait
 $CXX -shared -o "$OUT/libglintref.so" $objs "$OUT/compaction.o" "$OUT/ref_driver.o" -pthread -fopenmp -lm
+rm -f $objs "$OUT/compaction.o" "$OUT/ref_driver.o"
 echo "built $OUT/libglintref.so"
+
+# The reference's GPU kernels (cuda/geometry.cu, unmodified) as an sm_103a
+# cubin, and the byte layout of the structures they take, for
+# oracle/ref_gpu_driver.cpp.  Both are independent of the host CPU, so they
+# run on the GPU machine as built here.
+NVCC=${NVCC:-${CUDA_HOME:-/usr/local/cuda}/bin/nvcc}
+if [ -x "$NVCC" ]; then
+    $CXX -std=c++17 -O0 -w -I$HERE/ref_stub -I$SRC -I$CUDA_INC -pthread -fopenmp \
+        "$HERE/ref_gpu_layout.cpp" -o "$OUT/ref_gpu_layout"
+    "$OUT/ref_gpu_layout" > "$OUT/ref_gpu_layout.h"
+    rm -f "$OUT/ref_gpu_layout"
+    "$NVCC" -cubin -gencode arch=compute_103a,code=sm_103a -std=c++17 --extended-lambda -w \
+        -I$HERE/ref_stub -I$SRC "$SRC/cuda/geometry.cu" -o "$OUT/geometry.cubin"
+    echo "built $OUT/geometry.cubin"
+fi

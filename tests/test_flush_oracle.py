@@ -6,6 +6,7 @@ and CTF::binary_search / the search_SSTable walk reading the packed files.
 The reference produces the store only on its GPU path, which cannot run
 here, so the sort/STR/reduction steps are pinned by restatement only."""
 import ctypes
+import os
 
 import numpy as np
 import pytest
@@ -131,3 +132,46 @@ def test_flush_oversize_and_domain():
     box, flushes, st = run_store(flush_at=(39,), max_meet_time=8)
     assert flushes[0][1] == -4
     st.close()
+
+
+REF_GPU_GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_gpu_flush.npz")
+
+
+@pytest.mark.parametrize("case", ["dense_20k", "dense_20k_oversize", "small_100k", "collide_20k"])
+def test_flush_oracle_matches_reference_gpu_kernels(case):
+    """The flush restatement against the reference's OWN GPU kernels
+    (cuda_identify_meetings and process_with_gpu's flush, run from the
+    reference's unmodified geometry.cu; tests/golden/make_ref_gpu_golden.py):
+    every flush's packed keys, sids, capacities, CTF records, bitmaps and
+    oversize buffer, as digests, plus the counts."""
+    import make_ref_gpu_golden as G
+    from oracle.bindings import Store
+    g = np.load(REF_GPU_GOLDEN)
+    res = G.run_flush_case(case, Store, run_ref=False)
+    assert [r["t"] for r in res] == g[f"{case}/flush_steps"].tolist()
+    for k, r in enumerate(res):
+        assert G.info_tuple(r["oracle_info"]) == g[f"{case}/info"][k].tolist(), f"t={r['t']}"
+        assert G.flush_digests(r["oracle"]) == g[f"{case}/digests"][k].tolist(), f"t={r['t']}"
+
+
+@pytest.mark.parametrize("case", ["dense_20k", "reach_8k"])
+def test_active_search_oracle_matches_reference_gpu_kernel(case):
+    """The active multi-search restatement against the reference's own
+    cuda_identify_meetings search (cuda/geometry.cu:605-663) run on the GPU,
+    record multisets per step as digests."""
+    import make_ref_gpu_golden as G
+    from oracle.bindings import Oracle, make_config
+    from workloads import case_config, make_points
+    g = np.load(REF_GPU_GOLDEN)
+    steps, _ = G.SEARCH_CASES[case]
+    box, pts = make_points(case, steps)
+    cfgd = case_config(case)
+    o = Oracle(make_config(**cfgd), box, pts[0])
+    digs = []
+    for t in range(steps):
+        o.step(pts[t], t)
+        if t >= 8:
+            digs.append(G.digest(G.canonical_search(o.active_search(G.search_pids(case, t)))))
+    o.close()
+    assert digs == g[f"search/{case}/digests"].tolist()
+    assert int(g[f"search/{case}/counts"].sum()) > 0

@@ -95,3 +95,31 @@ def test_flush_outside_reference_domain_is_refused():
     with pytest.raises(GlintError):
         g.flush()
     g.close()
+
+
+@pytest.mark.parametrize("case", ["dense_20k", "dense_20k_oversize", "small_100k", "collide_20k"])
+def test_device_flush_matches_reference_gpu_kernels(case):
+    """The device flush against the reference's OWN GPU kernels on the same
+    workload (tests/golden/ref_gpu_flush.npz, made by running the
+    reference's unmodified geometry.cu flush): every flush's packed keys,
+    sids, capacities, CTF records, bitmaps and oversize buffer."""
+    import os
+
+    import make_ref_gpu_golden as G
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "ref_gpu_flush.npz"))
+    steps, flush_at, dprob, max_meet, split = G.FLUSH_CASES[case]
+    name = G.workload(case)
+    box, pts = make_points(name, steps)
+    dev = DeviceBench(gpu_bench(name, dProbFalse=dprob, max_meet_time=max_meet, CTF_count=split * split,
+                                split_num=split), box, pts[0])
+    k = 0
+    for t in range(steps):
+        dev.step(pts[t], t)
+        if t in flush_at:
+            dev.flush()
+            s = dev.store()
+            assert [int(getattr(s["info"], f)) for f in G.INFO] == g[f"{case}/info"][k].tolist(), f"t={t}"
+            assert G.flush_digests(s) == g[f"{case}/digests"][k].tolist(), f"t={t}"
+            k += 1
+    assert k == len(flush_at)
+    dev.close()
