@@ -15,7 +15,10 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libglintref.so")
-REFERENCE_ROOT = os.environ.get("GLINT_REFERENCE_ROOT", "/root/reference")
+# the reference checkout: GLINT_REFERENCE_ROOT, else a directory named
+# "reference" beside this repository
+REFERENCE_ROOT = os.environ.get("GLINT_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
+                                                                          "reference")
 
 
 def build_oracle() -> str:

@@ -3,7 +3,9 @@
 # they lie (never copied into this repository) plus oracle/ref_driver.cpp.
 # Test infrastructure only; the product never loads the result.
 #
-#   usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default /root/reference)
+#   usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   (default: $GLINT_REFERENCE_ROOT, else a directory named "reference"
+#   beside this repository)
 #
 # Flags: -O2 -ffp-contract=off so that FP64 expressions are evaluated with one
 # rounding per operation on every host (GCC contracts a*b+c into an FMA by
@@ -12,7 +14,7 @@
 # util/config.h includes but the CPU stages never call.
 set -eu
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${1:-/root/reference}
+REF=${1:-${GLINT_REFERENCE_ROOT:-$(cd "$HERE/../.." && pwd)/reference}}
 SRC="$REF/src"
 OUT="$HERE/_ref"
 if [ ! -d "$SRC/tracing" ]; then
