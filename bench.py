@@ -71,6 +71,15 @@ def parse():
     p.add_argument("--serve-sweep", default="50,2000",
                    help="further Poisson rates (req/s) served for --serve-seconds / 2 each; empty: none")
     p.add_argument("--no-serve", action="store_true")
+    p.add_argument("--serve-deadline", type=float, default=20.0,
+                   help="seconds after a stream's last arrival before its unfinished queries are given up")
+    p.add_argument("--serve-reserve-gb", type=float, default=8.0,
+                   help="device memory left free for the query slots when the store moves onto the device")
+    p.add_argument("--serve-steps", type=int, default=1800,
+                   help="steps of the serving store's build (the serving configuration: 10M objects x 1800 s)")
+    p.add_argument("--serve-device-gb", type=float, default=230.0, help="device memory for kept store blocks")
+    p.add_argument("--serve-host-gb", type=float, default=90.0,
+                   help="page-locked host memory for the kept store blocks before the device's")
     p.add_argument("--compact-split", type=int, default=56,
                    help="split_num of the compaction leg (the reference tool merges into 56^2 = 3136 CTFs)")
     p.add_argument("--compact-sample-objects", type=int, default=500_000)
@@ -518,10 +527,12 @@ def workload_config(args, N, form):
             "l2": "inputs larger than L2 (160 MB of points per step, 34 GB table)"}
 
 
-def poisson_stream(srv, rng, N, t_hi, rate, seconds):
+def poisson_stream(srv, rng, N, t_hi, rate, seconds, deadline_s):
     """queries arriving at `rate` for `seconds`, each submitted when it
-    arrives and retired when its last hop is done: latencies (ms), wall time
-    and objects reached"""
+    arrives and retired when its last hop is done; those not done
+    `deadline_s` after the last arrival are left unfinished (counted, not
+    waited for).  Returns latencies of the finished queries (ms), wall time,
+    objects reached, queries, unfinished"""
     n = max(1, int(rate * seconds))
     arrive = np.cumsum(rng.exponential(1.0 / rate, n))
     qs = []
@@ -534,8 +545,11 @@ def poisson_stream(srv, rng, N, t_hi, rate, seconds):
     lat, inflight, i = [], {}, 0
     reached = 0
     t_start = time.perf_counter()
+    stop_at = arrive[-1] + deadline_s
     while len(lat) < n:
         now = time.perf_counter() - t_start
+        if now > stop_at:
+            break
         while i < n and arrive[i] <= now:
             inflight[srv.submit(*qs[i])] = arrive[i]
             i += 1
@@ -550,7 +564,24 @@ def poisson_stream(srv, rng, N, t_hi, rate, seconds):
                 lat.append(done_t - inflight.pop(tk))
                 reached += r[2]
     wall = time.perf_counter() - t_start
-    return np.array(lat) * 1000.0, wall, reached, n
+    unfinished = n - len(lat)
+    # a server is not reused after a stream that left queries behind
+    return np.array(lat) * 1000.0, wall, reached, n, unfinished
+
+
+def latency_summary(lat, n, unfinished, deadline_s):
+    """p50/p99 over all arrivals: unfinished queries count as slower than any
+    finished one (p99 is null when more than 1% did not finish by the
+    deadline)"""
+    out = {"queries": n, "finished": n - unfinished, "deadline_s": deadline_s}
+    if unfinished == 0:
+        out.update({"p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))})
+        return out
+    srt = np.sort(lat)
+    for p in (50, 99):  # nearest rank over all arrivals; null past the finished ones
+        k = int(np.ceil(p / 100.0 * n)) - 1
+        out[f"p{p}_ms"] = float(srt[k]) if k < len(srt) else None
+    return out
 
 
 def serving(args, bench, N, t_hi, sweep_rates=True):
@@ -561,16 +592,29 @@ def serving(args, bench, N, t_hi, sweep_rates=True):
     if bench.store_blocks() == 0:
         return None
     rng = np.random.default_rng(0x474C494E54000005)
+    dl = args.serve_deadline
     srv = gp.Server(bench, max_slots=64)
-    lat, wall, reached, n = poisson_stream(srv, rng, N, t_hi, args.serve_rate, args.serve_seconds)
+    lat, wall, reached, n, unf = poisson_stream(srv, rng, N, t_hi, args.serve_rate, args.serve_seconds, dl)
+    main = latency_summary(lat, n, unf, dl)
     sweep = {}
-    for r in [float(x) for x in args.serve_sweep.split(",") if x.strip() and sweep_rates]:
-        sl, sw, _, sn = poisson_stream(srv, rng, N, t_hi, r, args.serve_seconds / 2)
-        sweep[f"{r:g}"] = {"queries": sn, "qps": sn / sw, "p50_ms": float(np.percentile(sl, 50)),
-                           "p99_ms": float(np.percentile(sl, 99))}
-    # 2-hop queries from 1000 seeds, one at a time
-    two = []
+    rates = [float(x) for x in args.serve_sweep.split(",") if x.strip() and sweep_rates]
+    left = unf
+    for r in rates:
+        if left:
+            srv.close()
+            srv = gp.Server(bench, max_slots=64)
+        sl, sw, _, sn, su = poisson_stream(srv, rng, N, t_hi, r, args.serve_seconds / 2, dl)
+        sweep[f"{r:g}"] = dict(latency_summary(sl, sn, su, dl), qps=(sn - su) / sw)
+        left = su
+    if left:
+        srv.close()
+        srv = gp.Server(bench, max_slots=64)
+    # 2-hop queries from 1000 seeds, one at a time, within --serve-deadline in total
+    two, two_reached = [], []
+    t_all = time.perf_counter()
     for _ in range(20):
+        if time.perf_counter() - t_all > dl:
+            break
         seeds = rng.choice(N, 1000, replace=False).astype(np.uint32)
         t0 = time.perf_counter()
         tk = srv.submit(seeds, 2)
@@ -579,14 +623,94 @@ def serving(args, bench, N, t_hi, sweep_rates=True):
             srv.step()
             r = srv.poll(tk, cap=1)
         two.append((time.perf_counter() - t0) * 1000.0)
+        two_reached.append(r[2])
     srv.close()
     two = np.array(two)
-    return {"queries": n, "rate_req_s": args.serve_rate, "qps": n / wall, "p50_ms": float(np.percentile(lat, 50)),
-            "p99_ms": float(np.percentile(lat, 99)), "slots": srv.slots, "store_blocks": bench.store_blocks(),
-            "mean_reached": reached / n, "rates": sweep,
-            "mix": "seeds 1-1000 log-uniform, 1-3 hops, window 10-1800 s log-uniform",
-            "two_hop_1k_seeds": {"p50_ms": float(np.percentile(two, 50)), "p99_ms": float(np.percentile(two, 99)),
-                                 "queries": len(two)}}
+    res = dict(main, rate_req_s=args.serve_rate, qps=(n - unf) / wall, slots=srv.slots,
+               store_blocks=bench.store_blocks(), mean_reached=reached / max(1, n - unf), rates=sweep,
+               mix="seeds 1-1000 log-uniform, 1-3 hops, window 10-1800 s log-uniform")
+    res["two_hop_1k_seeds"] = {"p50_ms": float(np.percentile(two, 50)) if len(two) else None,
+                               "p99_ms": float(np.percentile(two, 99)) if len(two) else None,
+                               "queries": len(two), "mean_reached": float(np.mean(two_reached)) if two_reached else None}
+    return res
+
+
+def serving_store(args, local, N, pb, ob, box, first):
+    """The serving configuration: a store built on the device from N objects
+    over --serve-steps steps of the same generator (auto flush past 2^26
+    keys), then the Poisson query stream against it.  The whole store does
+    not fit one GPU beside the meeting table (about 12.4M keys, 190 MB
+    packed, per step at 10M objects), so the most recent blocks stay on the
+    device and the ones before them in page-locked host memory, as far as
+    the --serve-device-gb / --serve-host-gb budgets go; older blocks are
+    dropped.  The line says how much of the history is served."""
+    import glint_pipeline_gb300 as gp
+    from glint_pipeline_gb300 import _abi
+    lib = _abi.lib()
+    rt = cudart()
+    rt.cudaSetDevice(local)
+    steps = args.serve_steps
+    free, total = ctypes.c_size_t(), ctypes.c_size_t()
+    rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total))
+    # a kept block: the packed keys of one window (2^26 keys plus one step's
+    # overshoot, about 15 bytes each) and 10 bytes per object of indexes
+    block_bytes = ((1 << 26) + 6_000_000) * 15 + 10 * N
+    ctx_bytes = 32 * args.buckets + 700 * N
+    dev_budget = min(args.serve_device_gb * 1e9, free.value - ctx_bytes - 20e9)
+    avail = host_memory_available() or 0
+    host_budget = min(args.serve_host_gb * 1e9, 0.45 * avail)
+    keep = max(1, int(dev_budget // block_bytes))
+    host_keep = max(0, int(host_budget // block_bytes))
+    cfg = gp.Configuration(num_objects=N, num_meeting_buckets=args.buckets, device=local, precision_mode=1,
+                           auto_flush=True, store_keep=keep, store_host_keep=host_keep)
+    bench = gp.DeviceBench(cfg, box, first)
+    gh = ctypes.c_void_p()
+    assert lib.glint_gen_create(pb, len(pb), ob, N, len(ob) // N, 0, ctypes.byref(gh)) == 0
+    buf = ctypes.c_void_p()
+    assert rt.cudaMalloc(ctypes.byref(buf), ctypes.c_size_t(16 * N)) == 0
+    flushes, keys_total = 0, 0
+    t0 = time.perf_counter()
+    try:
+        for t in range(steps):
+            lib.glint_gen_step(gh, buf, ctypes.c_void_p(bench.stream))
+            bench.step_device(buf.value, t)
+            st = bench.sync()
+            if st.error_flags:
+                raise RuntimeError(f"serving store build: step {t} error flags {st.error_flags:#x}")
+            if st.flushed:
+                flushes += 1
+                last = bench.block_info(bench.store_blocks() - 1).store
+                keys_total += int(last.kv_count) + int(last.oversize_kv_count)
+        build_s = time.perf_counter() - t0
+        lib.glint_gen_destroy(gh)
+        gh = None
+        rt.cudaFree(buf)
+        buf = None
+        # serving needs no meeting table: release the step state and bring
+        # the host-kept blocks onto the device
+        on_device = bench.serve_only(reserve=int(args.serve_reserve_gb * 1e9))
+        nb = bench.store_blocks()
+        infos = [bench.block_info(i).store for i in range(nb)]
+        kept_keys = sum(int(i.kv_count) + int(i.oversize_kv_count) for i in infos)
+        res = serving(args, bench, N, steps)
+        res["store"] = {"objects": N, "steps_built": steps, "build_s": build_s, "flushes": flushes,
+                        "blocks_kept": nb, "blocks_on_device_while_stepping": min(nb, keep),
+                        "blocks_on_device_serving": on_device, "blocks_in_host_memory_serving": nb - on_device,
+                        "keys_flushed": keys_total,
+                        "keys_kept": kept_keys,
+                        "history_fraction_kept": kept_keys / keys_total if keys_total else None,
+                        "steps_kept_from": min(int(i.end_time_min) for i in infos) if infos else None,
+                        "budgets_gb": {"device": dev_budget / 1e9, "host": host_budget / 1e9},
+                        "note": "while stepping the newest blocks stay on the device and the ones before them "
+                                "in page-locked host memory (older ones would be dropped); for serving the "
+                                "meeting table is released and host-kept blocks move onto the device"}
+        return res
+    finally:
+        if gh:
+            lib.glint_gen_destroy(gh)
+        if buf:
+            rt.cudaFree(buf)
+        bench.close()
 
 
 def compaction(args, bench):
@@ -993,8 +1117,6 @@ def main():
     for m in modes:
         forms[m] = run_form(args, m, N, local, pg, world, box, first, pb, ob, dbuf, step_bytes, rt)
         b = forms[m].pop("_bench")
-        if m == modes[0] and not args.no_serve:
-            serve = serving(args, b, N, total)
         if m == modes[0] and not args.no_compact:
             compact = compaction(args, b)
             if compact and "error" not in compact and not args.no_serve:
@@ -1003,6 +1125,11 @@ def main():
                 compact["serving"] = serving(args, b, N, total, sweep_rates=False)
         b.close()
     rt.cudaFree(dbuf)
+    if not args.no_serve and world == 1:
+        try:
+            serve = serving_store(args, local, N, pb, ob, box, first)
+        except Exception as e:  # reported in the line; the headline does not depend on it
+            serve = {"error": f"{type(e).__name__}: {e}"}
     head = forms[modes[0]]
     parity = {}
     if len(modes) == 2:

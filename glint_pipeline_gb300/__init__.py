@@ -61,6 +61,7 @@ class Configuration:
     auto_flush: bool = False
     split_num: int = 10
     store_keep: int = 16                # flushed blocks kept on the device for queries
+    store_host_keep: int = 0            # further blocks kept in page-locked host memory for queries
     use_graph: bool = False             # capture the step as a CUDA graph
     kv_restriction: int = 0             # 0 -> G_bytes * 2^25 keys (config.h:80)
     kv_capacity: int = 0                # 0 -> kv_restriction + max(1e6, 4 N)
@@ -192,6 +193,16 @@ class DeviceBench:
         if st != 0:
             raise GlintError(st, self.last_error())
         return info
+
+    def serve_only(self, reserve: int = 8 << 30) -> int:
+        """Keep only what queries need (glint_serve_only): the step state is
+        released and host-kept blocks move onto the device while `reserve`
+        bytes stay free; returns the blocks on the device."""
+        n = ctypes.c_uint32()
+        st = self.lib.glint_serve_only(self.h, int(reserve), ctypes.byref(n))
+        if st != 0:
+            raise GlintError(st, self.last_error())
+        return int(n.value)
 
     def store(self) -> dict:
         """The last flush's store as host arrays (the reference's h_keys,

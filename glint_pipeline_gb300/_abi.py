@@ -54,7 +54,7 @@ class GlintConfig(ctypes.Structure):
         ("kv_restriction", ctypes.c_uint64),
         ("kv_capacity", ctypes.c_uint64),
         ("use_graph", ctypes.c_uint32),
-        ("reserved2", ctypes.c_uint32),
+        ("store_host_keep", ctypes.c_uint32),
     ]
 
 
@@ -218,6 +218,7 @@ def load_library(path: str | None = None):
     lib.glint_stream.argtypes = [vp]
     lib.glint_active_search.argtypes = [vp, vp, u32, vp, u64, ctypes.POINTER(u64)]
     lib.glint_flush.argtypes = [vp, ctypes.POINTER(GlintStoreInfo)]
+    lib.glint_serve_only.argtypes = [vp, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint32)]
     lib.glint_query_batch.argtypes = [vp, ctypes.POINTER(GlintQuery), u32, ctypes.POINTER(GlintQueryResult)]
     lib.glint_store_blocks.restype = u32
     lib.glint_store_blocks.argtypes = [vp]

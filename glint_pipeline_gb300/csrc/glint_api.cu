@@ -748,12 +748,14 @@ glint_status glint_sync(glint_ctx *c, glint_step_stats *st) {
 
 glint_status glint_step_device(glint_ctx *c, const double *d_points, uint32_t cur_time) {
     if (!c || !d_points) return GLINT_ERR_INVALID_ARGUMENT;
+    if (serve_only_refused(c, "step")) return GLINT_ERR_STATE;
     cudaSetDevice(c->device);
     return enqueue_step(c, d_points, false, cur_time);
 }
 
 glint_status glint_step(glint_ctx *c, const double *points, uint32_t cur_time, glint_step_stats *st) {
     if (!c || !points) return GLINT_ERR_INVALID_ARGUMENT;
+    if (serve_only_refused(c, "step")) return GLINT_ERR_STATE;
     cudaSetDevice(c->device);
     glint_status r = enqueue_step(c, points, true, cur_time);
     if (r != GLINT_OK) return r;
@@ -778,6 +780,7 @@ glint_status glint_host_free(void *p) {
 
 glint_status glint_meetings(glint_ctx *c, glint_meeting *out, uint64_t cap, uint64_t *n) {
     if (!c) return GLINT_ERR_INVALID_ARGUMENT;
+    if (serve_only_refused(c, "meetings")) return GLINT_ERR_STATE;
     cudaError_t e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) return cuda_fail(c, e, "meetings");
     const uint64_t total = c->h_cnt->meetings;
@@ -833,6 +836,7 @@ glint_status glint_get_schema(glint_ctx *c, glint_schema_node *nodes, uint32_t *
 
 glint_status glint_get_buckets(glint_ctx *c, uint64_t *keys, uint32_t *starts, float *mbrs) {
     if (!c) return GLINT_ERR_INVALID_ARGUMENT;
+    if (serve_only_refused(c, "buckets")) return GLINT_ERR_STATE;
     cudaStreamSynchronize(c->stream);
     const uint64_t chunk = 1ull << 22;
     std::vector<TRec> buf((size_t)std::min<uint64_t>(chunk, c->B));

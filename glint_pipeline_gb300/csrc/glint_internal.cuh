@@ -111,8 +111,17 @@ struct StoreBlock {
     uint32_t o_times[4] = {0, 0, 0, 0};    /* oversize buffer start_time_min/max, end_time_min/max */
     uint32_t rec_times[4] = {0, 0, 0, 0};  /* the CTB record's own start/end time fields */
     uint32_t sid_count = 0, oversize_oid_count = 0;
+    bool on_host = false;                  /* arrays in page-locked host memory (read over the host link) */
+    uint32_t start_min = 0;                /* no key's meeting starts before this, and none ends after
+                                              end_time_max: a query window outside both finds nothing */
+    bool spans_known = false;              /* start_min and end_time_max were taken from the keys here
+                                              (flushed or merged blocks; not blocks read from files) */
 };
 void store_block_release(StoreBlock &b);
+/* the kept blocks after one was added: the oldest device blocks beyond
+ * store_keep move to host memory while fewer than store_host_keep are
+ * there; beyond that the oldest block is dropped */
+cudaError_t store_blocks_trim(glint_ctx *c);
 
 /* device-side descriptor of a StoreBlock */
 struct StoreBlockDev {
@@ -132,6 +141,8 @@ struct StepTimers {
 };
 
 glint_status enqueue_device_step_plain(glint_ctx *c, const double *d_points, uint32_t cur_time);
+/* true (and last_error set) when the context was turned to serving only */
+bool serve_only_refused(glint_ctx *c, const char *what);
 
 } // namespace glint
 
@@ -230,6 +241,7 @@ struct glint_ctx {
     glint_store_info store;
     std::vector<uint32_t> store_ctf_cap;
     bool store_valid = false;
+    bool serve_only = false;    /* glint_serve_only: the step state is gone, the kept blocks remain */
     ulonglong2 *store_keys_ptr = nullptr;
     float4 *store_boxes_ptr = nullptr;
     uint64_t store_kv = 0;

@@ -99,6 +99,7 @@ static glint_status pipe_finish(glint_pipe *p) {
 
 extern "C" glint_status glint_pipe_create(glint_ctx *c, uint64_t result_capacity, glint_pipe **out) {
     if (!c || !out) return GLINT_ERR_INVALID_ARGUMENT;
+    if (glint::serve_only_refused(c, "pipe")) return GLINT_ERR_STATE;
     *out = nullptr;
     cudaSetDevice(c->device);
     glint_pipe *p = new glint_pipe();

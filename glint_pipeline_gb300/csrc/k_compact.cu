@@ -672,7 +672,7 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
     for (uint32_t i = 0; i < count; ++i) {
         const StoreBlock &b = c->ctbs[first + i];
         std::vector<glint_ctf_meta> m(b.C);
-        if (b.C && (e = cudaMemcpy(m.data(), b.ctfs, sizeof(glint_ctf_meta) * b.C, cudaMemcpyDeviceToHost)) !=
+        if (b.C && (e = cudaMemcpy(m.data(), b.ctfs, sizeof(glint_ctf_meta) * b.C, cudaMemcpyDefault)) !=
                        cudaSuccess)
             return cuda_fail(e, "source CTFs");
         toffs[i].resize(b.C ? b.C : 1);
@@ -1037,6 +1037,13 @@ extern "C" glint_status glint_store_compact(glint_ctx *c, uint32_t first, uint32
     std::memcpy(nb.rec_times, rec, sizeof(rec));
     nb.sid_count = split;
     for (uint32_t o = 0; o < N; ++o) nb.oversize_oid_count += hsids[o] == 1;
+    nb.start_min = c->ctbs[first].start_min;
+    nb.spans_known = true;
+    for (uint32_t i = 0; i < count; ++i) {
+        nb.start_min = std::min(nb.start_min, c->ctbs[first + i].start_min);
+        nb.spans_known = nb.spans_known && c->ctbs[first + i].spans_known &&
+                         c->ctbs[first + i].end_time_max <= last_time;
+    }
     /* the new block takes the merged blocks' place (servers read the kept
      * blocks from their own streams) */
     cudaDeviceSynchronize();

@@ -692,6 +692,19 @@ __global__ void k_ctf_pack(const u128 *__restrict__ keys, const float4 *__restri
 
 /* where each object's keys sit in a flushed block: its CTF part index or its
  * oversize-buffer index, and how many */
+/* the earliest meeting start among n unpacked keys (low word: duration << 32
+ * | end - base) */
+__global__ void k_keys_min_start(const ulonglong2 *__restrict__ keys, uint64_t n, uint32_t base,
+                                 uint32_t *__restrict__ out) {
+    uint32_t m = 0xffffffffu;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const unsigned long long x = keys[i].x;
+        m = min(m, (uint32_t)x + base - (uint32_t)(x >> 32));
+    }
+    for (int o = 16; o > 0; o >>= 1) m = min(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if ((threadIdx.x & 31) == 0 && m != 0xffffffffu) atomicMin(out, m);
+}
+
 __global__ void k_block_index(uint32_t N, const uint32_t *__restrict__ seg_of, const uint32_t *__restrict__ same,
                               const uint8_t *__restrict__ over, uint64_t kv, uint32_t *__restrict__ first,
                               uint32_t *__restrict__ count) {
@@ -1046,6 +1059,24 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
         cudaMemcpyAsync(b.bitmaps, c->d_bitmaps, (size_t)C * kBitCount / 8, cudaMemcpyDeviceToDevice, s);
         cudaMemcpyAsync(b.obitmap, c->d_obitmap, kBitCount / 8, cudaMemcpyDeviceToDevice, s);
         k_block_index<<<grid_for(N, 256), 256, 0, s>>>(N, c->d_segof, c->d_same, c->d_over, kv, b.first, b.count);
+        /* the block's earliest meeting start, for queries that skip blocks
+         * outside their time window; the low half of the key count word
+         * (cleared right after the keep) holds it meanwhile */
+        {
+            uint32_t *d_min = reinterpret_cast<uint32_t *>(&c->d_cnt->kv_count);
+            cudaMemsetAsync(d_min, 0xff, sizeof(uint32_t), s);
+            if (kv + o_n)
+                k_keys_min_start<<<grid_for(kv + o_n, 256, 152u * 8u), 256, 0, s>>>(
+                    reinterpret_cast<const ulonglong2 *>(c->d_keys), kv + o_n, c->end_time_min, d_min);
+            uint32_t m = 0;
+            cudaMemcpyAsync(&m, d_min, sizeof(uint32_t), cudaMemcpyDeviceToHost, s);
+            if ((ae = cudaStreamSynchronize(s)) != cudaSuccess) {
+                store_block_release(b);
+                return fail(ae, "keep block");
+            }
+            b.start_min = (kv + o_n) ? m : 0;
+            b.spans_known = true;
+        }
         b.kv = kv;
         b.o_count = o_n;
         b.key_bytes = bytes;
@@ -1059,11 +1090,7 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
         b.sid_count = inf.sid_count;
         b.oversize_oid_count = inf.oversize_oid_count;
         c->ctbs.push_back(b);
-        while (c->ctbs.size() > c->cfg.store_keep) {
-            cudaStreamSynchronize(s);
-            store_block_release(c->ctbs.front());
-            c->ctbs.erase(c->ctbs.begin());
-        }
+        if ((ae = store_blocks_trim(c)) != cudaSuccess) return fail(ae, "keep block in host memory");
     }
 
     /* the next window (cuda/geometry.cu:2112-2131, tracing/process.cpp:271,549);
@@ -1087,8 +1114,73 @@ glint_status run_flush(glint_ctx *c, glint_store_info *info, std::string &err) {
 
 } // namespace glint
 
+/* glint_serve_only: the meeting table, the meeting log and the pending-key
+ * buffers are released; host-kept blocks move back to the device, oldest
+ * first, while more than `reserve` bytes stay free */
+extern "C" glint_status glint_serve_only(glint_ctx *c, uint64_t reserve, uint32_t *blocks_on_device) {
+    if (!c) return GLINT_ERR_INVALID_ARGUMENT;
+    cudaSetDevice(c->device);
+    cudaError_t e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        c->last_error = std::string("serve only: ") + cudaGetErrorString(e);
+        return GLINT_ERR_CUDA;
+    }
+    if (!c->serve_only) {
+        void **big[] = {(void **)&c->d_tab, (void **)&c->d_stamp, (void **)&c->d_newline, (void **)&c->d_new,
+                        (void **)&c->d_log, (void **)&c->d_keys, (void **)&c->d_keys2, (void **)&c->d_kvbox,
+                        (void **)&c->d_kvbox2, (void **)&c->d_ctf_keys};
+        for (void **p : big) {
+            if (*p) cudaFree(*p);
+            *p = nullptr;
+        }
+        c->serve_only = true;
+        c->store_valid = false;
+        c->stats_valid = false;
+    }
+    const size_t N = c->N;
+    for (StoreBlock &b : c->ctbs) {
+        if (!b.on_host) continue;
+        void **fields[] = {(void **)&b.keys, (void **)&b.ctfs, (void **)&b.key_index, (void **)&b.byte_index,
+                           (void **)&b.sids, (void **)&b.first, (void **)&b.count, (void **)&b.okeys,
+                           (void **)&b.oboxes, (void **)&b.bitmaps, (void **)&b.obitmap};
+        const size_t bytes[] = {b.key_bytes ? b.key_bytes : 1, sizeof(glint_ctf_meta) * b.C,
+                                sizeof(unsigned long long) * b.C, sizeof(unsigned long long) * b.C,
+                                sizeof(uint16_t) * N, sizeof(uint32_t) * N, sizeof(uint32_t) * N,
+                                sizeof(ulonglong2) * b.o_count, sizeof(float4) * b.o_count,
+                                (size_t)b.C * kBitCount / 8, kBitCount / 8};
+        constexpr int F = sizeof(bytes) / sizeof(bytes[0]);
+        size_t total = 0, free_b = 0, all_b = 0;
+        for (size_t x : bytes) total += x;
+        if (cudaMemGetInfo(&free_b, &all_b) != cudaSuccess || free_b < total + reserve) break;
+        void *dev[F] = {};
+        e = cudaSuccess;
+        for (int i = 0; i < F && e == cudaSuccess; ++i) e = cudaMalloc(&dev[i], bytes[i] ? bytes[i] : 1);
+        for (int i = 0; i < F && e == cudaSuccess; ++i)
+            if (bytes[i] && *fields[i]) e = cudaMemcpyAsync(dev[i], *fields[i], bytes[i], cudaMemcpyHostToDevice, c->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+        if (e != cudaSuccess) {
+            for (int i = 0; i < F; ++i)
+                if (dev[i]) cudaFree(dev[i]);
+            cudaGetLastError();
+            break;
+        }
+        for (int i = 0; i < F; ++i) {
+            if (*fields[i]) cudaFreeHost(*fields[i]);
+            *fields[i] = dev[i];
+        }
+        b.on_host = false;
+    }
+    if (blocks_on_device) {
+        uint32_t n = 0;
+        for (const StoreBlock &b : c->ctbs) n += b.on_host ? 0u : 1u;
+        *blocks_on_device = n;
+    }
+    return GLINT_OK;
+}
+
 extern "C" glint_status glint_flush(glint_ctx *c, glint_store_info *info) {
     if (!c) return GLINT_ERR_INVALID_ARGUMENT;
+    if (serve_only_refused(c, "flush")) return GLINT_ERR_STATE;
     if (c->step_index == 0) {
         c->last_error = "flush before the first step";
         return GLINT_ERR_STATE;
@@ -1146,8 +1238,101 @@ void store_block_release(StoreBlock &b) {
     void *ps[] = {b.keys,  b.ctfs,  b.key_index, b.byte_index, b.sids,   b.first,
                   b.count, b.okeys, b.oboxes,    b.bitmaps,    b.obitmap};
     for (void *p : ps)
-        if (p) cudaFree(p);
+        if (p) {
+            if (b.on_host) cudaFreeHost(p);
+            else cudaFree(p);
+        }
     b = StoreBlock();
+}
+
+/* a device-kept block's arrays into page-locked host memory.  On this
+ * platform a page-locked allocation is addressed by the GPU at its host
+ * address (unified addressing), so the block's pointers stay valid for the
+ * query kernels; where the device address differs, or host memory runs
+ * out, the block is not moved (moved = false). */
+static cudaError_t block_to_host(glint_ctx *c, StoreBlock &b, bool &moved) {
+    moved = false;
+    const size_t N = c->N;
+    void **fields[] = {(void **)&b.keys, (void **)&b.ctfs, (void **)&b.key_index, (void **)&b.byte_index,
+                       (void **)&b.sids, (void **)&b.first, (void **)&b.count, (void **)&b.okeys,
+                       (void **)&b.oboxes, (void **)&b.bitmaps, (void **)&b.obitmap};
+    const size_t bytes[] = {b.key_bytes ? b.key_bytes : 1, sizeof(glint_ctf_meta) * b.C,
+                            sizeof(unsigned long long) * b.C, sizeof(unsigned long long) * b.C,
+                            sizeof(uint16_t) * N, sizeof(uint32_t) * N, sizeof(uint32_t) * N,
+                            sizeof(ulonglong2) * b.o_count, sizeof(float4) * b.o_count,
+                            (size_t)b.C * kBitCount / 8, kBitCount / 8};
+    constexpr int F = sizeof(bytes) / sizeof(bytes[0]);
+    void *host[F] = {};
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < F && e == cudaSuccess; ++i) {
+        e = cudaHostAlloc(&host[i], bytes[i] ? bytes[i] : 1, cudaHostAllocMapped);
+        void *dp = nullptr;
+        if (e == cudaSuccess) e = cudaHostGetDevicePointer(&dp, host[i], 0);
+        if (e == cudaSuccess && dp != host[i]) e = cudaErrorNotSupported;
+    }
+    for (int i = 0; i < F && e == cudaSuccess; ++i)
+        if (bytes[i] && *fields[i]) e = cudaMemcpyAsync(host[i], *fields[i], bytes[i], cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        for (int i = 0; i < F; ++i)
+            if (host[i]) cudaFreeHost(host[i]);
+        if (e == cudaErrorNotSupported || e == cudaErrorMemoryAllocation) {
+            cudaGetLastError();
+            return cudaSuccess;
+        }
+        return e;
+    }
+    for (int i = 0; i < F; ++i) {
+        if (*fields[i]) cudaFree(*fields[i]);
+        *fields[i] = host[i];
+    }
+    b.on_host = true;
+    moved = true;
+    return cudaSuccess;
+}
+
+bool serve_only_refused(glint_ctx *c, const char *what) {
+    if (!c->serve_only) return false;
+    c->last_error = std::string(what) + ": the context serves queries only (glint_serve_only)";
+    return true;
+}
+
+cudaError_t store_blocks_trim(glint_ctx *c) {
+    /* kept blocks run oldest to newest */
+    for (;;) {
+        size_t host = 0, dev = 0, oldest_dev = c->ctbs.size();
+        for (size_t i = 0; i < c->ctbs.size(); ++i) {
+            if (c->ctbs[i].on_host) {
+                ++host;
+            } else {
+                if (oldest_dev == c->ctbs.size()) oldest_dev = i;
+                ++dev;
+            }
+        }
+        if (host > c->cfg.store_host_keep) {
+            /* the oldest host-kept block goes */
+            for (size_t i = 0; i < c->ctbs.size(); ++i)
+                if (c->ctbs[i].on_host) {
+                    store_block_release(c->ctbs[i]);
+                    c->ctbs.erase(c->ctbs.begin() + (long)i);
+                    break;
+                }
+            continue;
+        }
+        if (dev <= c->cfg.store_keep) break;
+        cudaStreamSynchronize(c->stream);
+        bool moved = false;
+        if (c->cfg.store_host_keep) {
+            cudaError_t e = block_to_host(c, c->ctbs[oldest_dev], moved);
+            if (e != cudaSuccess) return e;
+        }
+        if (!moved) {
+            /* no host tier, or no room for it there: the oldest device block goes */
+            store_block_release(c->ctbs[oldest_dev]);
+            c->ctbs.erase(c->ctbs.begin() + (long)oldest_dev);
+        }
+    }
+    return cudaSuccess;
 }
 
 void store_blocks_free(glint_ctx *c) {

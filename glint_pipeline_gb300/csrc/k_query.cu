@@ -203,6 +203,7 @@ cudaError_t grow(T **p, uint64_t &have, uint64_t need) {
 extern "C" glint_status glint_active_search(glint_ctx *c, const uint32_t *pids, uint32_t npids, glint_search_info *out,
                                             uint64_t cap, uint64_t *n) {
     if (!c || (npids && !pids) || (cap && !out)) return GLINT_ERR_INVALID_ARGUMENT;
+    if (serve_only_refused(c, "active search")) return GLINT_ERR_STATE;
     if (c->step_index == 0) {
         c->last_error = "active search before the first step";
         return GLINT_ERR_STATE;
@@ -316,6 +317,7 @@ cudaError_t noalloc_setup(int device) {
 extern "C" glint_status glint_active_search_noalloc(glint_ctx *c, const uint32_t *d_pids, uint32_t npids,
                                                     glint_search_info *d_out, uint64_t cap, uint64_t *d_n) {
     if (!c || (npids && !d_pids) || (cap && !d_out) || !d_n) return GLINT_ERR_INVALID_ARGUMENT;
+    if (serve_only_refused(c, "active search")) return GLINT_ERR_STATE;
     if (c->step_index == 0) {
         c->last_error = "active search before the first step";
         return GLINT_ERR_STATE;

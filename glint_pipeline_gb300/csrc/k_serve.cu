@@ -11,7 +11,8 @@
  *
  * Device form: every query owns a slot, a visited bitmap over objects and
  * two object lists (frontier, next).  One launch advances every active slot
- * by one hop: its items are (slot, frontier object, kept block) triples; the
+ * by one hop: its items are (slot, frontier object, kept block) triples,
+ * over the kept blocks whose time span can meet the slot's window; the
  * object's sid, first and count in the block locate its keys, which are
  * decoded as CTF::parse_key does (tracing/step_merge.cpp:335-345), and each
  * target inside the time window that the slot has not visited joins its next
@@ -47,7 +48,9 @@ struct HopArgs {
     uint32_t *counts;                      /* [slot] next-list sizes */
     unsigned long long *scanned;           /* [slot] keys read */
     const uint32_t *active;                /* [A] slots taking part in this launch */
-    const unsigned long long *prefix;      /* [A + 1] their frontier sizes, prefix sums */
+    const unsigned long long *prefix;      /* [A + 1] their items (frontier x blocks), prefix sums */
+    const uint32_t *rel;                   /* each active slot's blocks, concatenated */
+    const uint32_t *rel_off;               /* [A + 1] where each active slot's blocks start in rel */
     uint32_t A;
 };
 
@@ -59,8 +62,11 @@ __device__ inline void visit(const HopArgs &a, uint32_t s, uint32_t next_list, u
     const unsigned calling = __activemask();
     bool fresh = false;
     if (target < a.N) {
+        /* a query's bits only go from 0 to 1, so a set bit read from L2 is
+         * final and saves the atomic; a clear one is settled by the atomic */
         const uint32_t bit = 1u << (target & 31);
-        fresh = !(atomicOr(&a.visited[(size_t)s * a.words + (target >> 5)], bit) & bit);
+        uint32_t *w = &a.visited[(size_t)s * a.words + (target >> 5)];
+        if (!(__ldcg(w) & bit)) fresh = !(atomicOr(w, bit) & bit);
     }
     const unsigned appending = __ballot_sync(calling, fresh);
     if (!fresh) return;
@@ -74,20 +80,27 @@ __device__ inline void visit(const HopArgs &a, uint32_t s, uint32_t next_list, u
 }
 
 __global__ void __launch_bounds__(256) k_serve_hop(HopArgs a) {
-    const unsigned long long total = a.prefix[a.A] * a.nblocks;
+    const unsigned long long total = a.prefix[a.A];
     for (unsigned long long it = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; it < total;
          it += (unsigned long long)gridDim.x * blockDim.x) {
-        const unsigned long long f = it / a.nblocks;
-        const uint32_t b = (uint32_t)(it - f * a.nblocks);
-        uint32_t lo = 0, hi = a.A; /* prefix[lo] <= f < prefix[lo + 1] */
+        uint32_t lo = 0, hi = a.A; /* prefix[lo] <= it < prefix[lo + 1] */
         while (hi - lo > 1) {
             const uint32_t mid = (lo + hi) / 2;
-            if (a.prefix[mid] <= f) lo = mid;
+            if (a.prefix[mid] <= it) lo = mid;
             else hi = mid;
         }
+        /* block-major within a slot: consecutive items take consecutive
+         * frontier objects (ascending ids) of one block, whose sids,
+         * key ranges and keys then lie close together */
+        const uint32_t nrel = a.rel_off[lo + 1] - a.rel_off[lo];
+        const unsigned long long fr = (a.prefix[lo + 1] - a.prefix[lo]) / nrel;
+        const unsigned long long local = it - a.prefix[lo];
+        const unsigned long long bi = local / fr;
+        const unsigned long long f = local - bi * fr;
+        const uint32_t b = a.rel[a.rel_off[lo] + (uint32_t)bi];
         const uint32_t s = a.active[lo];
         const SlotParam sp = a.param[s];
-        const uint32_t obj = a.lists[((size_t)s * 2 + sp.cur) * a.N + (f - a.prefix[lo])];
+        const uint32_t obj = a.lists[((size_t)s * 2 + sp.cur) * a.N + f];
         const StoreBlockDev blk = a.blocks[b];
         const uint32_t sid = blk.sids[obj];
         if (sid == 0) continue;
@@ -209,6 +222,8 @@ struct glint_server {
     uint64_t seeds_cap = 0;
     StoreBlockDev *blocks = nullptr;
     uint32_t blocks_cap = 0;
+    uint32_t *rel = nullptr, *rel_off = nullptr;   /* each active slot's blocks (the window's) */
+    uint64_t rel_cap = 0, rel_off_cap = 0;
     uint64_t next_ticket = 1;
     std::deque<PendingQuery> queue;
     std::vector<SlotState> state;
@@ -225,7 +240,7 @@ struct glint_server {
 static void server_release(glint_server *v) {
     void *ps[] = {v->visited, v->lists, v->counts, v->active, v->seed_slots, v->param, v->scanned, v->prefix,
                   v->sprefix, v->seeds, v->blocks, v->rk, v->rk2, v->roff, v->rv, v->rv2, v->rids, v->rs_tmp,
-                  v->rscan};
+                  v->rscan, v->rel, v->rel_off};
     for (void *p : ps)
         if (p) cudaFree(p);
 }
@@ -344,6 +359,8 @@ static HopArgs server_args(glint_server *v, uint32_t nb) {
     a.scanned = v->scanned;
     a.active = v->active;
     a.prefix = v->prefix;
+    a.rel = v->rel;
+    a.rel_off = v->rel_off;
     a.A = 0;
     return a;
 }
@@ -423,23 +440,57 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
         for (uint32_t k : admitted) v->state[k].frontier = cnt[k];
     }
 
-    /* one hop for every active slot */
-    std::vector<uint32_t> act;
+    /* one hop for every active slot, over the kept blocks that can hold a
+     * key inside its window: a key of a block ends at most at end_time_max
+     * and starts no earlier than start_min, and it counts when
+     * start < t_end and t_start < end */
+    std::vector<uint32_t> act, rel;
+    std::vector<uint32_t> rel_off(1, 0);
     std::vector<unsigned long long> prefix(1, 0);
     for (uint32_t k = 0; k < v->slots; ++k) {
         const SlotState &st = v->state[k];
         if (!st.busy || st.hop >= st.hops) continue;
         act.push_back(k);
-        prefix.push_back(prefix.back() + st.frontier);
+        const SlotParam &sp = v->hparam[k];
+        uint32_t nrel = 0;
+        for (uint32_t i = 0; i < nb; ++i) {
+            const StoreBlock &b = c->ctbs[i];
+            if (sp.window && b.spans_known && !(b.start_min < sp.t_end && sp.t_start < b.end_time_max)) continue;
+            rel.push_back(i);
+            ++nrel;
+        }
+        rel_off.push_back((uint32_t)rel.size());
+        prefix.push_back(prefix.back() + (unsigned long long)st.frontier * nrel);
     }
     if (!act.empty()) {
+        if (v->rel_cap < rel.size() + 1) {
+            if (v->rel) cudaFree(v->rel);
+            v->rel = nullptr;
+            v->rel_cap = 0;
+            if ((e = cudaMalloc((void **)&v->rel, sizeof(uint32_t) * (rel.size() + 1))) != cudaSuccess)
+                return server_fail(v, e, "blocks of the windows");
+            v->rel_cap = rel.size() + 1;
+        }
+        if (v->rel_off_cap < rel_off.size()) {
+            if (v->rel_off) cudaFree(v->rel_off);
+            v->rel_off = nullptr;
+            v->rel_off_cap = 0;
+            if ((e = cudaMalloc((void **)&v->rel_off, sizeof(uint32_t) * rel_off.size())) != cudaSuccess)
+                return server_fail(v, e, "blocks of the windows");
+            v->rel_off_cap = rel_off.size();
+        }
+        a.rel = v->rel;
+        a.rel_off = v->rel_off;
         cudaMemcpyAsync(v->param, v->hparam.data(), sizeof(SlotParam) * v->slots, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(v->active, act.data(), sizeof(uint32_t) * act.size(), cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(v->prefix, prefix.data(), sizeof(unsigned long long) * prefix.size(), cudaMemcpyHostToDevice,
                         s);
+        if (!rel.empty())
+            cudaMemcpyAsync(v->rel, rel.data(), sizeof(uint32_t) * rel.size(), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(v->rel_off, rel_off.data(), sizeof(uint32_t) * rel_off.size(), cudaMemcpyHostToDevice, s);
         for (uint32_t k : act) cudaMemsetAsync(v->counts + k, 0, sizeof(uint32_t), s);
         a.A = (uint32_t)act.size();
-        const unsigned long long items = prefix.back() * nb;
+        const unsigned long long items = prefix.back();
         if (items) k_serve_hop<<<grid_for(items, 256, 152u * 16u), 256, 0, s>>>(a);
         std::vector<uint32_t> cnt(v->slots);
         std::vector<unsigned long long> scanned(v->slots);
@@ -545,6 +596,7 @@ void servers_detach(glint_ctx *c) {
         v->param = nullptr;
         v->scanned = v->prefix = v->sprefix = nullptr;
         v->blocks = nullptr;
+        v->rel = v->rel_off = nullptr;
         v->ctx = nullptr;
     }
     c->servers.clear();

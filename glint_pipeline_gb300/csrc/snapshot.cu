@@ -73,7 +73,7 @@ struct Writer {
     cudaError_t dev(uint32_t tag, const void *d, size_t bytes) {
         section(tag, bytes);
         std::vector<uint8_t> h(bytes);
-        cudaError_t e = bytes ? cudaMemcpy(h.data(), d, bytes, cudaMemcpyDeviceToHost) : cudaSuccess;
+        cudaError_t e = bytes ? cudaMemcpy(h.data(), d, bytes, cudaMemcpyDefault) : cudaSuccess;
         raw(h.data(), bytes);
         return e;
     }
@@ -129,6 +129,7 @@ glint_status snap_fail(glint_ctx *c, cudaError_t e) {
 
 extern "C" glint_status glint_snapshot_save(glint_ctx *c, const char *path) {
     if (!c || !path) return GLINT_ERR_INVALID_ARGUMENT;
+    if (serve_only_refused(c, "snapshot")) return GLINT_ERR_STATE;
     if (c->step_index == 0) {
         c->last_error = "snapshot: before the first step";
         return GLINT_ERR_STATE;

@@ -381,10 +381,10 @@ extern "C" glint_status glint_store_dump(glint_ctx *c, const char *raid_path, co
  * store_keep) */
 static glint_status keep_block(glint_ctx *c, StoreBlock &b) {
     c->ctbs.push_back(b);
-    while (c->ctbs.size() > c->cfg.store_keep) {
-        cudaStreamSynchronize(c->stream);
-        store_block_release(c->ctbs.front());
-        c->ctbs.erase(c->ctbs.begin());
+    const cudaError_t e = store_blocks_trim(c);
+    if (e != cudaSuccess) {
+        c->last_error = std::string("store load: keeping the block: ") + cudaGetErrorString(e);
+        return GLINT_ERR_CUDA;
     }
     return GLINT_OK;
 }
@@ -501,7 +501,7 @@ extern "C" glint_status glint_store_block_read(glint_ctx *c, uint32_t block, uin
     cudaError_t e = cudaStreamSynchronize(c->stream);
     const StoreBlock &b = c->ctbs[block];
     auto down = [&](void *dst, const void *src, size_t n) {
-        if (e == cudaSuccess && dst && n) e = cudaMemcpy(dst, src, n, cudaMemcpyDeviceToHost);
+        if (e == cudaSuccess && dst && n) e = cudaMemcpy(dst, src, n, cudaMemcpyDefault);
     };
     down(keys, b.keys, b.key_bytes);
     down(sids, b.sids, sizeof(uint16_t) * (size_t)c->N);

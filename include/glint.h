@@ -97,7 +97,9 @@ typedef struct glint_config {
                                       (util/config.h:81 adds 1000000) */
     uint32_t use_graph;            /* 1: capture the step once as a CUDA graph and replay it (device
                                       input buffer only; per-stage timing off) */
-    uint32_t reserved2;
+    uint32_t store_host_keep;      /* further blocks kept in page-locked host memory, which the GPU reads
+                                      over the host link: the oldest device-kept block moves there when
+                                      a new one arrives beyond store_keep; 0 -> none */
 } glint_config;
 
 typedef struct glint_box {
@@ -328,6 +330,15 @@ typedef struct glint_store_info {
  * or CTF capacities that do not add up to the key count (meetings longer
  * than max_meet_time shift the reference's CTF ranges). */
 glint_status glint_flush(glint_ctx *ctx, glint_store_info *info);
+/* No counterpart in the reference (its query tools read blocks from disk).
+ * Turns a context into a query server for the blocks it keeps: the meeting
+ * table, meeting log and pending-key buffers are released (GLINT_ERR_STATE
+ * from then on for steps, flushes, meetings, buckets, active searches,
+ * snapshots and pipes), and blocks kept in host memory move onto the device,
+ * oldest first, while more than `reserve` bytes of device memory stay free
+ * (for the servers' slots).  *blocks_on_device receives how many kept blocks
+ * are on the device afterwards.  May be called again to retry the move. */
+glint_status glint_serve_only(glint_ctx *ctx, uint64_t reserve, uint32_t *blocks_on_device);
 /* The last flush's store, into host arrays (any may be NULL): keys
  * (info.key_bytes), sids (num_objects u16, workbench::h_sids), ctf_capacity
  * and ctfs (CTF_count each), bitmaps (CTF_count * 8192 bytes), the oversize

@@ -10,13 +10,14 @@ from workloads import case_config, make_points
 pytestmark = pytest.mark.gpu
 
 
-def build_store(name, steps, flush_at, keep=16):
+def build_store(name, steps, flush_at, keep=16, host_keep=0):
     box, pts = make_points(name, steps)
     cfgd = case_config(name)
     c = Configuration(num_objects=cfgd["num_objects"], grid_capacity=cfgd["grid_capacity"],
                       grid_amplify=cfgd["grid_amplify"], num_meeting_buckets=cfgd["num_meeting_buckets"],
                       reach_distance=cfgd["reach_distance"], min_meet_time=cfgd["min_meet_time"],
-                      schema_update_delay=cfgd["schema_update_delay"], kv_capacity=1 << 22, store_keep=keep)
+                      schema_update_delay=cfgd["schema_update_delay"], kv_capacity=1 << 22, store_keep=keep,
+                      store_host_keep=host_keep)
     g = DeviceBench(c, box, pts[0])
     g.map_box = np.asarray(box, np.float64)
     windows = []   # meetings of each flushed window
@@ -71,6 +72,46 @@ def test_query_matches_oracle_bfs():
     big = [(rng.choice(n, 20, replace=False).astype(np.uint32), 2, 0, 0) for _ in range(70)]
     check(g, n, edges, big)
     g.close()
+
+
+def test_query_over_host_kept_blocks():
+    """blocks beyond store_keep move to page-locked host memory (up to
+    store_host_keep) and are still queried, read by the GPU over the host
+    link; beyond both the oldest block is dropped.  Queries, block reads and
+    a compaction over a mix of host- and device-kept blocks agree with the
+    oracle and with an all-device context."""
+    flush_at = (10, 16, 22, 28, 34, 39)
+    g, n, windows = build_store("dense_20k", 40, flush_at, keep=2, host_keep=3)
+    assert g.store_blocks() == 5
+    edges = edges_of(np.concatenate(windows[1:]), g.map_box)
+    rng = np.random.default_rng(6)
+    queries = [(rng.choice(n, k, replace=False).astype(np.uint32), hops, 0, 0) for k, hops in
+               ((1, 3), (40, 2), (500, 3))] + [(rng.choice(n, 60, replace=False).astype(np.uint32), 2, 12, 30)]
+    check(g, n, edges, queries)
+    ref, _, _ = build_store("dense_20k", 40, flush_at, keep=5)
+    assert ref.store_blocks() == 5
+    for i in range(5):
+        a, b = g.block(i), ref.block(i)
+        for k in ("sids", "keys", "bitmaps", "o_keys"):
+            assert np.array_equal(a[k], b[k]), (i, k)
+    # serving only: the step state goes, the host-kept blocks move onto the
+    # device, queries answer as before and steps are refused
+    got_before, _ = g.query(queries)
+    assert g.serve_only(reserve=1 << 30) == 5
+    got_after, _ = g.query(queries)
+    for a, b in zip(got_before, got_after):
+        for h in range(len(a)):
+            np.testing.assert_array_equal(a[h], b[h])
+    box, pts = make_points("dense_20k", 41)
+    with pytest.raises(Exception):
+        g.step(pts[40], 40)
+    info_g = g.compact(0, 5, 4)
+    info_r = ref.compact(0, 5, 4)
+    assert info_g["kv_count"] == info_r["kv_count"]
+    for k in ("sids", "keys", "bitmaps", "o_keys"):
+        assert np.array_equal(g.block(0)[k], ref.block(0)[k]), k
+    g.close()
+    ref.close()
 
 
 def test_query_kept_blocks_only():
