@@ -126,6 +126,7 @@ cudaError_t store_blocks_trim(glint_ctx *c);
 /* device-side descriptor of a StoreBlock */
 struct StoreBlockDev {
     const uint8_t *keys;
+    unsigned long long key_bytes;
     const glint_ctf_meta *ctfs;
     const unsigned long long *key_index, *byte_index;
     const uint16_t *sids;

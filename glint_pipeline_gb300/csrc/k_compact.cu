@@ -107,22 +107,6 @@ __global__ void k_cmp_tables(const glint_ctf_meta *__restrict__ ctfs, const uint
         td[o.z + v] = __dmul_rn(__ddiv_rn(__ull2double_rn(v), __ull2double_rn(me)), (double)le);
 }
 
-/* kb <= 16 little-endian bytes at p; whole words where they stay inside the
- * buffer */
-__device__ inline u128 load_key(const uint8_t *p, uint32_t kb, const uint8_t *end) {
-    const uintptr_t a = (uintptr_t)p;
-    const uint64_t *w = (const uint64_t *)(a & ~(uintptr_t)7);
-    const uint32_t sh = (uint32_t)(a & 7) * 8;
-    u128 v;
-    if ((const uint8_t *)(w + 3) <= end) {
-        const uint64_t w0 = w[0], w1 = w[1];
-        v = ((u128)w1 << 64 | w0) >> sh;
-        if (sh) v |= (u128)w[2] << (128 - sh);
-    } else {
-        return get_key_bytes(p, kb);
-    }
-    return kb < 16 ? v & (((u128)1 << (8 * kb)) - 1) : v;
-}
 
 __global__ void __launch_bounds__(256) k_cmp_parse(const SrcBlock *__restrict__ src, uint32_t nsrc, uint64_t R,
                                                    uint32_t N, const float *__restrict__ tf,

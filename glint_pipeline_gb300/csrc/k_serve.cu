@@ -81,6 +81,10 @@ __device__ inline void visit(const HopArgs &a, uint32_t s, uint32_t next_list, u
 
 __global__ void __launch_bounds__(256) k_serve_hop(HopArgs a) {
     const unsigned long long total = a.prefix[a.A];
+    /* keys read, per slot: summed here while this thread's items stay in one
+     * slot (slots own contiguous item ranges), added once when they move on */
+    uint32_t acc_slot = 0xffffffffu;
+    unsigned long long acc = 0;
     for (unsigned long long it = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; it < total;
          it += (unsigned long long)gridDim.x * blockDim.x) {
         uint32_t lo = 0, hi = a.A; /* prefix[lo] <= it < prefix[lo + 1] */
@@ -106,7 +110,12 @@ __global__ void __launch_bounds__(256) k_serve_hop(HopArgs a) {
         if (sid == 0) continue;
         const uint32_t n = blk.count[obj], first = blk.first[obj];
         const uint32_t nl = sp.cur ^ 1u;
-        if (n) atomicAdd(&a.scanned[s], (unsigned long long)n);
+        if (s != acc_slot) {
+            if (acc) atomicAdd(&a.scanned[acc_slot], acc);
+            acc_slot = s;
+            acc = 0;
+        }
+        acc += n;
         if (sid == 1) {
             for (uint32_t j = 0; j < n; ++j) {
                 const ulonglong2 k = blk.okeys[first + j];
@@ -124,7 +133,7 @@ __global__ void __launch_bounds__(256) k_serve_hop(HopArgs a) {
         const uint8_t *base = blk.keys + blk.byte_index[c] + (unsigned long long)(first - blk.key_index[c]) * kb;
         for (uint32_t j = 0; j < n; ++j) {
             const uint8_t *p = base + (size_t)j * kb;
-            unsigned __int128 v = get_key_bytes(p, kb);
+            unsigned __int128 v = load_key(p, kb, blk.keys + blk.key_bytes);
             v >>= m.mbr_bit;
             const uint32_t end = (uint32_t)(v & ((1ull << m.end_bit) - 1)) + blk.end_time_min;
             v >>= m.end_bit;
@@ -136,6 +145,7 @@ __global__ void __launch_bounds__(256) k_serve_hop(HopArgs a) {
             visit(a, s, nl, target);
         }
     }
+    if (acc) atomicAdd(&a.scanned[acc_slot], acc);
 }
 
 /* the new ids of the active slots as (slot rank, id) keys: slot rank r's
@@ -386,8 +396,8 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
     std::vector<StoreBlockDev> bd(nb);
     for (uint32_t i = 0; i < nb; ++i) {
         const StoreBlock &b = c->ctbs[i];
-        bd[i] = StoreBlockDev{b.keys, b.ctfs, b.key_index, b.byte_index, b.sids, b.first, b.count, b.okeys,
-                              b.end_time_min, b.C};
+        bd[i] = StoreBlockDev{b.keys, b.key_bytes, b.ctfs, b.key_index, b.byte_index, b.sids, b.first, b.count,
+                              b.okeys, b.end_time_min, b.C};
     }
     if (nb) cudaMemcpyAsync(v->blocks, bd.data(), sizeof(StoreBlockDev) * nb, cudaMemcpyHostToDevice, s);
     HopArgs a = server_args(v, nb);

@@ -49,6 +49,24 @@ __device__ inline unsigned __int128 get_key_bytes(const uint8_t *src, uint32_t k
     return ((unsigned __int128)hi << 64) | lo;
 }
 
+/* kb <= 16 little-endian bytes at p, read as whole 8-byte words where
+ * they stay inside the buffer ending at `end` (whose start is 8-aligned),
+ * else byte by byte */
+__device__ inline unsigned __int128 load_key(const uint8_t *p, uint32_t kb, const uint8_t *end) {
+    const uintptr_t a = (uintptr_t)p;
+    const uint64_t *w = (const uint64_t *)(a & ~(uintptr_t)7);
+    const uint32_t sh = (uint32_t)(a & 7) * 8;
+    unsigned __int128 v;
+    if ((const uint8_t *)(w + 3) <= end) {
+        const uint64_t w0 = w[0], w1 = w[1];
+        v = ((unsigned __int128)w1 << 64 | w0) >> sh;
+        if (sh) v |= (unsigned __int128)w[2] << (128 - sh);
+    } else {
+        return get_key_bytes(p, kb);
+    }
+    return kb < 16 ? v & (((unsigned __int128)1 << (8 * kb)) - 1) : v;
+}
+
 } // namespace glint
 
 #endif
