@@ -795,9 +795,10 @@ def next_pow2(v):
 def run_batch(args, local):
     """Batching form: R regions, populations log-uniform in [1k, 2M], each with
     its own generator seed, street grid and hotspots, advanced together
-    (glint_batch_*: per-region streams, captured step graphs) against the
-    same regions stepped one after another without graphs; an autotuner picks
-    leaf capacity and hash load factor per size class for a tuned run."""
+    (glint_batch_*: one graph per timestep, one refine launch over all
+    regions) against the same regions stepped one after another without
+    graphs; an autotuner picks leaf capacity, hash load factor and refine tile
+    width per size class for a tuned run."""
     import glint_pipeline_gb300 as gp
     from glint_pipeline_gb300 import _abi
     from glint_pipeline_gb300.batch import Batch, autotune
@@ -830,10 +831,11 @@ def run_batch(args, local):
         assert rt.cudaMalloc(ctypes.byref(inp), ctypes.c_size_t(16 * n)) == 0
         regions.append({"n": n, "box": box, "first": first, "steps": buf, "input": inp})
 
-    def config(n, cap=50, lf=None):
+    def config(n, cap=50, lf=None, chunk=0):
         b = next_pow2(int(64 * n)) if lf is None else next_pow2(int(28 * n / lf))
         return gp.Configuration(num_objects=n, num_meeting_buckets=b, grid_capacity=cap, precision_mode=1,
-                                auto_flush=True, kv_restriction=max(1 << 20, 8 * n), store_keep=2, device=local)
+                                auto_flush=True, kv_restriction=max(1 << 20, 8 * n), store_keep=2, device=local,
+                                refine_chunk=chunk)
 
     def copy_in(t, streams):
         for r, reg in enumerate(regions):
@@ -904,15 +906,16 @@ def run_batch(args, local):
             dt = (time.perf_counter() - t0) / 3
             b.close()
             return dt
-        best, table = autotune(lambda cap, lf, n=rep["n"]: config(n, cap, lf), trial,
-                               capacities=(32, 50, 128, 512), load_factors=(0.5, 0.9))
-        picks[f"{lo}-{hi}"] = {"capacity": best[0], "load_factor": best[1]}
+        best, table = autotune(lambda cap, lf, ch, n=rep["n"]: config(n, cap, lf, ch), trial,
+                               capacities=(32, 50, 128, 512, 1024), load_factors=(0.5, 0.9),
+                               chunks=(64, 128, 256, 512))
+        picks[f"{lo}-{hi}"] = {"capacity": best[0], "load_factor": best[1], "refine_chunk": best[2]}
         tables[f"{lo}-{hi}"] = table
     tuned_cfgs = []
     for x in regions:
         key = next(f"{lo}-{hi}" for lo, hi in classes if lo <= x["n"] < hi)
         p = picks[key]
-        tuned_cfgs.append(config(x["n"], p["capacity"], p["load_factor"]))
+        tuned_cfgs.append(config(x["n"], p["capacity"], p["load_factor"], p["refine_chunk"]))
     t_tuned, _ = batched(tuned_cfgs)
     for x in regions:
         rt.cudaFree(x["steps"])

@@ -62,6 +62,7 @@ class Configuration:
     split_num: int = 10
     store_keep: int = 16                # flushed blocks kept on the device for queries
     store_host_keep: int = 0            # further blocks kept in page-locked host memory for queries
+    refine_chunk: int = 0               # cross-leaf checks per refine work item; 0 -> 64
     use_graph: bool = False             # capture the step as a CUDA graph
     kv_restriction: int = 0             # 0 -> G_bytes * 2^25 keys (config.h:80)
     kv_capacity: int = 0                # 0 -> kv_restriction + max(1e6, 4 N)

@@ -55,6 +55,8 @@ class GlintConfig(ctypes.Structure):
         ("kv_capacity", ctypes.c_uint64),
         ("use_graph", ctypes.c_uint32),
         ("store_host_keep", ctypes.c_uint32),
+        ("refine_chunk", ctypes.c_uint32),
+        ("reserved3", ctypes.c_uint32),
     ]
 
 

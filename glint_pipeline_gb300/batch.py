@@ -1,8 +1,10 @@
 """Batching form: many independent regions advanced together on one GPU
 (glint_batch_*), and a small autotuner for per-region settings.
 
-Each region is its own context; its step runs as a captured CUDA graph on its
-own stream, and every region's step is launched before any is waited for.
+Each region is its own context with its own stream.  A timestep of the whole
+batch is one captured CUDA graph: every region's stages up to the refine
+stage side by side, one refine launch over the work items of every region in
+the FP32-screen form, then every region's remaining stages.
 """
 from __future__ import annotations
 
@@ -67,21 +69,34 @@ class Batch:
             pass
 
 
-def autotune(make_config, run_trial, capacities=(32, 50, 128, 512, 1024), load_factors=(0.5, 0.7, 0.9)):
-    """Pick (leaf capacity, hash load factor) for one region by timing short
-    trials.  make_config(capacity, load_factor) -> Configuration;
-    run_trial(config) -> seconds per step.  Returns (best, table)."""
+def autotune(make_config, run_trial, capacities=(32, 50, 128, 512, 1024), load_factors=(0.5, 0.7, 0.9),
+             chunks=(64, 128, 256, 512)):
+    """Pick (leaf capacity, hash load factor, refine tile width) for one
+    region by timing short trials: capacity x load factor at the default
+    tile width first, then the tile widths at the best pair.
+    make_config(capacity, load_factor, chunk) -> Configuration;
+    run_trial(config) -> seconds per step.  Returns ((capacity, load_factor,
+    chunk, seconds), table)."""
     table = []
+
+    def trial(cap, lf, chunk):
+        t0 = time.perf_counter()
+        try:
+            sec = run_trial(make_config(cap, lf, chunk))
+        except GlintError:
+            sec = float("inf")
+        table.append({"capacity": cap, "load_factor": lf, "refine_chunk": chunk, "sec_per_step": sec,
+                      "trial_s": time.perf_counter() - t0})
+        return sec
+
     best = None
     for cap in capacities:
         for lf in load_factors:
-            t0 = time.perf_counter()
-            try:
-                sec = run_trial(make_config(cap, lf))
-            except GlintError:
-                sec = float("inf")
-            table.append({"capacity": cap, "load_factor": lf, "sec_per_step": sec,
-                          "trial_s": time.perf_counter() - t0})
-            if best is None or sec < best[2]:
-                best = (cap, lf, sec)
+            sec = trial(cap, lf, chunks[0])
+            if best is None or sec < best[3]:
+                best = (cap, lf, chunks[0], sec)
+    for chunk in chunks[1:]:
+        sec = trial(best[0], best[1], chunk)
+        if sec < best[3]:
+            best = (best[0], best[1], chunk, sec)
     return best, table

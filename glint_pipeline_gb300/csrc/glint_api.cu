@@ -302,7 +302,8 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     if (!cfg_in || !mbr || !out) return GLINT_ERR_INVALID_ARGUMENT;
     *out = nullptr;
     glint_config cfg = *cfg_in;
-    if (cfg.num_objects == 0 || cfg.grid_capacity == 0 || cfg.reach_distance <= 0) return GLINT_ERR_INVALID_ARGUMENT;
+    if (cfg.num_objects == 0 || cfg.grid_capacity == 0 || cfg.reach_distance <= 0 || cfg.refine_chunk > 65536)
+        return GLINT_ERR_INVALID_ARGUMENT;
     if (cfg.num_objects >= (1u << 26)) return GLINT_ERR_UNSUPPORTED;   /* OID_BIT = 26, util/util.h:49 */
     if (!cfg.phased_lookup) return GLINT_ERR_UNSUPPORTED;
     if (!init && !first_points) return GLINT_ERR_INVALID_ARGUMENT;
@@ -347,6 +348,7 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     const uint32_t N = cfg.num_objects;
     c->N = N;
     c->cap = (uint32_t)(cfg.grid_amplify * cfg.grid_capacity);
+    c->chunk = cfg.refine_chunk ? cfg.refine_chunk : kCrossChunk;
     const uint32_t per = N / cfg.grid_capacity;
     c->G = 4 * std::max<uint32_t>(100000u, per);
     c->S = (uint32_t)(1.6 * c->G);
@@ -435,8 +437,8 @@ glint_status glint_create(const glint_config *cfg_in, const glint_box *mbr, cons
     ALLOC(c->d_stamp, stamp_bytes(c->B));
     ALLOC(c->d_newline, newline_words(c->B));
     ALLOC(c->d_new, c->new_cap);
-    /* each extra refine item is a further kCrossChunk checks of one leaf */
-    c->rextra_cap = c->check_cap / kCrossChunk + 1;
+    /* each extra refine item is a further `chunk` checks of one leaf */
+    c->rextra_cap = c->check_cap / c->chunk + 1;
     ALLOC(c->d_rextra, c->rextra_cap);
     ALLOC(c->d_tile_cnt, c->n_tiles + 1);
     ALLOC(c->d_tile_off, c->n_tiles + 1);
@@ -589,9 +591,16 @@ glint_status glint_get_capacities(const glint_ctx *c, uint32_t *sc, uint32_t *gc
     return GLINT_OK;
 }
 
-/* the launches of one step, from the counter reset to the copy of the
- * counters to the host; no host synchronisation, so it can be captured */
-static void launch_step(glint_ctx *c, const double *points, bool host) {
+} // extern "C"
+
+namespace glint {
+
+/* The launches of one step, from the counter reset to the copy of the
+ * counters to the host; no host synchronisation, so they can be captured.
+ * A step is its front (up to the refine stage's work items), the refine
+ * pair tests, and its back: a batch of regions runs every front, then one
+ * refine launch over all regions, then every back. */
+void launch_step_front(glint_ctx *c, const double *points, bool host) {
     cudaStream_t s = c->stream;
     const bool tm = c->cfg.timing != 0 && !c->cfg.use_graph;
     cudaMemsetAsync(c->d_cnt, 0, kStepCounterBytes, s);
@@ -607,7 +616,12 @@ static void launch_step(glint_ctx *c, const double *points, bool host) {
     if (tm) cudaEventRecord(c->timers.ev[2], s);
     launch_filter(c);
     if (tm) cudaEventRecord(c->timers.ev[3], s);
-    launch_refine(c, 0);
+    launch_refine_items(c);
+}
+
+void launch_step_back(glint_ctx *c) {
+    cudaStream_t s = c->stream;
+    const bool tm = c->cfg.timing != 0 && !c->cfg.use_graph;
     if (tm) cudaEventRecord(c->timers.ev[4], s);
     launch_insert(c, 0);
     if (tm) cudaEventRecord(c->timers.ev[5], s);
@@ -631,18 +645,34 @@ static void launch_step(glint_ctx *c, const double *points, bool host) {
     cudaMemcpyAsync(c->h_cnt, c->d_cnt, sizeof(DevCounters), cudaMemcpyDeviceToHost, s);
 }
 
-static glint_status enqueue_step(glint_ctx *c, const double *points, bool host, uint32_t cur_time,
-                                 bool allow_graph = true) {
-    cudaStream_t s = c->stream;
-    /* a captured step reads its parameters from host memory when it runs:
-     * the previous step must have finished before they are overwritten */
-    if (c->cfg.use_graph && c->step_index > 0) cudaStreamSynchronize(s);
+static void launch_step(glint_ctx *c, const double *points, bool host) {
+    launch_step_front(c, points, host);
+    launch_refine_pairs(c);
+    launch_step_back(c);
+}
+
+/* the host side of starting a step: its number, time, tag and the
+ * parameters the captured memcpy reads when the step runs */
+void begin_step(glint_ctx *c, uint32_t cur_time) {
     c->step_index++;
     c->last_time = cur_time;
     c->h_params->step_time = cur_time;
     c->h_params->step_tag = stamp_of(c->step_index);
     c->h_params->end_time_min = c->end_time_min;
     c->stats_valid = false;
+}
+
+} // namespace glint
+
+extern "C" {
+
+static glint_status enqueue_step(glint_ctx *c, const double *points, bool host, uint32_t cur_time,
+                                 bool allow_graph = true) {
+    cudaStream_t s = c->stream;
+    /* a captured step reads its parameters from host memory when it runs:
+     * the previous step must have finished before they are overwritten */
+    if (c->cfg.use_graph && c->step_index > 0) cudaStreamSynchronize(s);
+    begin_step(c, cur_time);
     if (!c->cfg.use_graph || host || !allow_graph) {
         launch_step(c, points, host);
     } else {

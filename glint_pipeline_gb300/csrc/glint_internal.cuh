@@ -80,7 +80,8 @@ struct StepParams {
 constexpr size_t kStepCounterBytes = offsetof(DevCounters, ssi);
 
 /* cross-leaf checks per refine work item (refine_common.cuh) */
-constexpr uint32_t kCrossChunk = 64;
+constexpr uint32_t kCrossChunk = 64;       /* default cross-leaf checks per refine work item */
+constexpr size_t kMaxBlockSmem = 232448;   /* dynamic shared memory one block may use on sm_103a (227 KB) */
 
 struct NewEntry {
     unsigned long long key;
@@ -159,6 +160,7 @@ struct glint_ctx {
     std::string last_error;
 
     uint32_t N = 0, G = 0, S = 0, cap = 0;
+    uint32_t chunk = 64;        /* cross-leaf checks per refine work item */
     uint64_t B = 0, Bm = 0;
     uint64_t check_cap = 0, new_cap = 0, log_cap = 0;
     uint32_t max_leaf_count = 0;           /* sorter limit for one leaf segment */
@@ -291,6 +293,15 @@ void init_sin_coef(SinCoef *host);
 cudaError_t launch_partition(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_filter(glint_ctx *c);
 cudaError_t launch_refine(glint_ctx *c, uint32_t cur_time);
+cudaError_t launch_refine_items(glint_ctx *c);
+cudaError_t launch_refine_pairs(glint_ctx *c);
+struct RefineArgs;
+RefineArgs refine_args(glint_ctx *c);
+cudaError_t launch_refine_precision_batch(const RefineArgs *d_args, uint32_t R, uint32_t cap_max, uint32_t *ex_off,
+                                          uint32_t *wk_off, unsigned int *next, cudaStream_t s);
+void launch_step_front(glint_ctx *c, const double *points, bool host);
+void launch_step_back(glint_ctx *c);
+void begin_step(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_insert(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_identify(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_schema_update(glint_ctx *c, cudaStream_t s, void *scan_tmp);

@@ -23,6 +23,7 @@
  * id is dropped when the other test also passes, so every pair has at most
  * one event per step.
  */
+#include <algorithm>
 #include <atomic>
 
 #include "refine_common.cuh"
@@ -142,20 +143,27 @@ __global__ void __launch_bounds__(32 * kRefineWarps) k_refine_fp64(RefineArgs a)
     }
 }
 
-size_t refine_smem_bytes(uint32_t cap) {
+/* shared memory per warp (its leaf's members and its contact queue), and the
+ * warps per block that fit the per-block limit (large leaf buffers run with
+ * fewer warps per block) */
+static size_t refine_warp_bytes(uint32_t cap) {
     const size_t per_warp = (size_t)cap * 28 + sizeof(QEntry) * kQueue + 64;
-    return (size_t)kRefineWarps * ((per_warp + 63) & ~(size_t)63);
+    return (per_warp + 63) & ~(size_t)63;
 }
+int refine_warps(uint32_t cap) {
+    return (int)std::max<size_t>(1, std::min<size_t>(kRefineWarps, kMaxBlockSmem / refine_warp_bytes(cap)));
+}
+size_t refine_smem_bytes(uint32_t cap) { return (size_t)refine_warps(cap) * refine_warp_bytes(cap); }
 
 /* the chunks beyond the first of every leaf's cross-leaf checks */
 __global__ void __launch_bounds__(256) k_refine_extra(const uint32_t *__restrict__ work,
                                                       const uint32_t *__restrict__ tstart, uint2 *__restrict__ extra,
-                                                      uint64_t cap, DevCounters *cnt) {
+                                                      uint64_t cap, uint32_t per_item, DevCounters *cnt) {
     const uint32_t nwork = cnt->n_leaf_work;
     for (uint32_t li = blockIdx.x * blockDim.x + threadIdx.x; li < nwork; li += gridDim.x * blockDim.x) {
         const uint32_t g = work[li];
         const uint32_t cross = tstart[g + 1] - tstart[g];
-        const uint32_t chunks = (cross + kCrossChunk - 1) / kCrossChunk;
+        const uint32_t chunks = (cross + per_item - 1) / per_item;
         for (uint32_t ch = 1; ch < chunks; ++ch) {
             const uint32_t idx = atomicAdd(&cnt->n_extra, 1u);
             if (idx < cap) extra[idx] = make_uint2(g, ch);
@@ -190,6 +198,8 @@ RefineArgs refine_args(glint_ctx *c) {
     a.Bm = c->Bm;
     a.new_cap = c->new_cap;
     a.cap = c->cap;
+    a.chunk = c->chunk;
+    a.extra_cap = (uint32_t)std::min<uint64_t>(c->rextra_cap, 0xffffffffu);
     a.ex = make_exact(c);
     a.cnt = c->d_cnt;
     return a;
@@ -197,25 +207,32 @@ RefineArgs refine_args(glint_ctx *c) {
 
 cudaError_t launch_refine_precision(glint_ctx *c, const RefineArgs &a);
 
-cudaError_t launch_refine(glint_ctx *c, uint32_t /*cur_time*/) {
-    RefineArgs a = refine_args(c);
+/* the refine stage's work items: each leaf's chunks beyond its first */
+cudaError_t launch_refine_items(glint_ctx *c) {
     k_refine_extra<<<grid_for(c->G, 256), 256, 0, c->stream>>>(c->d_leaf_work, c->d_tstart, c->d_rextra,
-                                                               c->rextra_cap, c->d_cnt);
-    if (c->cfg.precision_mode == 1) return launch_refine_precision(c, a);
-    k_refine_fp64<<<152 * 8, 32 * kRefineWarps, refine_smem_bytes(c->cap), c->stream>>>(a);
+                                                               c->rextra_cap, c->chunk, c->d_cnt);
     return cudaGetLastError();
 }
 
+/* the refine stage's pair tests over its work items */
+cudaError_t launch_refine_pairs(glint_ctx *c) {
+    RefineArgs a = refine_args(c);
+    if (c->cfg.precision_mode == 1) return launch_refine_precision(c, a);
+    k_refine_fp64<<<152 * 8, 32 * refine_warps(c->cap), refine_smem_bytes(c->cap), c->stream>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_refine(glint_ctx *c, uint32_t /*cur_time*/) {
+    cudaError_t e = launch_refine_items(c);
+    return e != cudaSuccess ? e : launch_refine_pairs(c);
+}
+
 /* The limit is a property of the kernel, shared by every context of the
- * process: it only ever grows, to the largest leaf buffer asked for, so that
- * creating a context with a small buffer never breaks one with a larger. */
+ * process: it is set to the per-block maximum, and every launch asks for the
+ * shared memory its leaf buffer needs. */
 void refine_set_attributes(uint32_t cap) {
-    static std::atomic<uint32_t> largest{0};
-    uint32_t m = largest.load();
-    while (cap > m && !largest.compare_exchange_weak(m, cap)) {
-    }
-    const uint32_t use = cap > m ? cap : m;
-    cudaFuncSetAttribute(k_refine_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)refine_smem_bytes(use));
+    (void)cap;
+    cudaFuncSetAttribute(k_refine_fp64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kMaxBlockSmem);
 }
 
 /* ---- insertion of the step's new pairs -------------------------------------

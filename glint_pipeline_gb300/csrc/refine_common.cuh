@@ -42,6 +42,8 @@ struct RefineArgs {
     NewEntry *newlist;
     uint64_t B, Bm, new_cap;
     uint32_t cap;
+    uint32_t chunk;            /* cross-leaf checks per work item */
+    uint32_t extra_cap;        /* entries of `extra` */
     Frame f;
     ExactCtx ex;
     DevCounters *cnt;
@@ -156,7 +158,7 @@ __device__ inline void enqueue(const RefineArgs &a, QEntry *Q, uint32_t &qn, boo
     }
 }
 
-/* Work items: a leaf's inside pairs with its first kCrossChunk cross-leaf
+/* Work items: a leaf's inside pairs with its first `chunk` cross-leaf
  * checks, and one item per further chunk of its checks.  Dense leaves are
  * the target of thousands of checks; split into chunks they spread over the
  * warps instead of leaving a long tail on one.  Every event carries its
@@ -170,7 +172,7 @@ __device__ inline bool claim_item(const RefineArgs &a, uint32_t nwork, uint32_t 
     if (lane == 0) {
         if (!extra_done) {
             v = atomicAdd(&a.cnt->extra_next, 1u);
-            if (v < n_extra) kind = 1;
+            if (v < n_extra && v < a.extra_cap) kind = 1;
         }
         if (kind == 0) {
             v = atomicAdd(&a.cnt->work_next, 1u);
@@ -197,8 +199,8 @@ __device__ inline bool claim_item(const RefineArgs &a, uint32_t nwork, uint32_t 
 /* the cross-leaf checks of one item */
 __device__ inline void item_checks(const RefineArgs &a, uint32_t g, uint32_t chunk, uint32_t &tb, uint32_t &te) {
     const uint32_t b = a.tstart[g], e = a.tstart[g + 1];
-    tb = b + chunk * kCrossChunk;
-    te = tb + kCrossChunk < e ? tb + kCrossChunk : e;
+    tb = b + chunk * a.chunk;
+    te = tb + a.chunk < e ? tb + a.chunk : e;
     if (tb > e) tb = e;
 }
 

@@ -100,6 +100,9 @@ typedef struct glint_config {
     uint32_t store_host_keep;      /* further blocks kept in page-locked host memory, which the GPU reads
                                       over the host link: the oldest device-kept block moves there when
                                       a new one arrives beyond store_keep; 0 -> none */
+    uint32_t refine_chunk;         /* cross-leaf checks per refine work item (the refine tile width);
+                                      results do not depend on it; 0 -> 64 */
+    uint32_t reserved3;
 } glint_config;
 
 typedef struct glint_box {
@@ -569,14 +572,19 @@ typedef struct glint_precision_report {
 glint_status glint_precision_probe(glint_ctx *ctx, uint32_t stride, glint_precision_report *out);
 
 /* ---- batching form: many independent regions on one GPU ------------------
- * Each region is a context created from cfgs[r] (its step captured as a CUDA
- * graph, per-stage timing off) with its own stream.  glint_batch_step
- * launches every region's step for cur_time, reading d_points[r] (device
- * memory; keep the same buffer per region so the captured graph is reused),
- * and returns without waiting; glint_batch_sync waits for all of them and
- * runs each region's automatic flush, filling stats[r] when stats is not
- * NULL.  glint_batch_region gives a region's context for its meetings,
- * store and queries. */
+ * Each region is a context created from cfgs[r] (per-stage timing off; all on
+ * the same device) with its own stream.  glint_batch_step enqueues one
+ * timestep of every region for cur_time, reading d_points[r] (device memory),
+ * as one CUDA graph captured at the first step: every region's stages up to
+ * the refine stage, one refine launch over the work items of all regions in
+ * precision_mode 1 (regions in mode 0 refine on their own streams), then
+ * every region's remaining stages.  Keep the same buffers so the graph is
+ * reused; it is captured again when a pointer changes.  The call returns
+ * without waiting (after the previous timestep is done); glint_batch_sync
+ * waits for it and runs each region's automatic flush, filling stats[r] when
+ * stats is not NULL.  glint_batch_region gives a region's context for its
+ * meetings, store and queries; work queued on a region's stream runs before
+ * the batch's next timestep. */
 typedef struct glint_batch glint_batch;
 glint_status glint_batch_create(uint32_t num_regions, const glint_config *cfgs, const glint_box *mbrs,
                                 const double *const *first_points, glint_batch **out);
