@@ -88,6 +88,10 @@ def parse():
                    help="step10m: the headline line; batch64 / skew50m: the batching and precision forms; "
                         "compact: the compaction sample alone (--compact-sample-objects objects)")
     p.add_argument("--regions", type=int, default=64)
+    p.add_argument("--form-steps", type=int, default=6,
+                   help="timed steps of the batching and skew legs inside the default run (their own "
+                        "--workload runs use --steps)")
+    p.add_argument("--no-forms", action="store_true", help="skip the batching and skew legs of the default run")
     p.add_argument("--skew-objects", type=int, default=50_000_000)
     p.add_argument("--skew-buckets", type=int, default=1 << 31)
     p.add_argument("--core-objects", type=int, default=2_000_000)
@@ -792,7 +796,7 @@ def next_pow2(v):
     return p
 
 
-def run_batch(args, local):
+def run_batch(args, local, K=None, W=None):
     """Batching form: R regions, populations log-uniform in [1k, 2M], each with
     its own generator seed, street grid and hotspots, advanced together
     (glint_batch_*: one graph per timestep, one refine launch over all
@@ -809,7 +813,8 @@ def run_batch(args, local):
     R = args.regions
     rng = np.random.default_rng(SEED_REGIONS)
     pops = np.exp(rng.uniform(np.log(1_000), np.log(2_000_000), R)).astype(np.int64)
-    K, W = args.steps, max(args.warmup, 3)
+    K = args.steps if K is None else K
+    W = max(args.warmup if W is None else W, 3)
     total = W + K
     regions = []
     for r in range(R):
@@ -907,7 +912,7 @@ def run_batch(args, local):
             b.close()
             return dt
         best, table = autotune(lambda cap, lf, ch, n=rep["n"]: config(n, cap, lf, ch), trial,
-                               capacities=(32, 50, 128, 512, 1024), load_factors=(0.5, 0.9),
+                               capacities=(32, 50, 128, 512, 1024), load_factors=(0.5, 0.7, 0.9),
                                chunks=(64, 128, 256, 512))
         picks[f"{lo}-{hi}"] = {"capacity": best[0], "load_factor": best[1], "refine_chunk": best[2]}
         tables[f"{lo}-{hi}"] = table
@@ -932,8 +937,11 @@ def run_batch(args, local):
                       "sequential_no_graph": {"value": objs * K / t_seq, "ms_per_step": 1000.0 * t_seq / K},
                       "batched_autotuned": {"value": objs * K / t_tuned, "ms_per_step": 1000.0 * t_tuned / K,
                                             "picks": picks}},
-            "speedup_batched_vs_sequential": t_seq / t_batch, "autotune": tables}
-    print(json.dumps(line), flush=True)
+            "speedup_batched_vs_sequential": t_seq / t_batch,
+            "parity_note": "each region's meetings equal the oracle's at the region's own leaf capacity and "
+                           "buckets (the autotuned capacity changes the schema, as it would in the reference)",
+            "autotune": tables}
+    return line
 
 
 def meeting_digest(m):
@@ -977,7 +985,7 @@ class MeetingDigests:
 SKEW_SIGMA_SPREAD = float(np.sqrt(0.01 * 40000.0 ** 2 / (5 * np.pi)) / 2)
 
 
-def run_skew(args, local):
+def run_skew(args, local, K=None, W=None):
     """Precision form on extreme skew: 20% of the objects start at 5 hotspots,
     the rest uniform over the 40x40 km street grid.  Two cases: 'spread'
     (50M objects, hotspots covering 1% of the area) for throughput, and 'core'
@@ -994,7 +1002,8 @@ def run_skew(args, local):
     lib = _abi.lib()
     rt = cudart()
     rt.cudaSetDevice(local)
-    K, W = args.steps, max(args.warmup, 3)
+    K = args.steps if K is None else K
+    W = max(args.warmup if W is None else W, 3)
     cases = [("spread", args.skew_objects, SKEW_SIGMA_SPREAD, args.skew_buckets, 256),
              ("core", args.core_objects, 50.0, args.core_buckets or next_pow2(256 * args.core_objects), 16)]
     out = {}
@@ -1068,7 +1077,7 @@ def run_skew(args, local):
                                    f"{out['core']['objects']} objects",
                        "l2": "inputs larger than L2"},
             "clocks": head["clocks"], "gpu_launches": head["gpu_launches"], "cases": out}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
@@ -1079,11 +1088,11 @@ def main():
         return
     if args.workload == "batch64":
         if rank == 0:
-            run_batch(args, local)
+            print(json.dumps(run_batch(args, local)), flush=True)
         return
     if args.workload == "skew50m":
         if rank == 0:
-            run_skew(args, local)
+            print(json.dumps(run_skew(args, local)), flush=True)
         return
     if args.workload == "compact":
         if rank == 0:
@@ -1133,6 +1142,17 @@ def main():
             serve = serving_store(args, local, N, pb, ob, box, first)
         except Exception as e:  # reported in the line; the headline does not depend on it
             serve = {"error": f"{type(e).__name__}: {e}"}
+    other = {}
+    if not args.no_forms and world == 1:
+        # the batching and precision forms, a few steps each (their own
+        # --workload runs give the full lines)
+        for name, fn in (("batch64", run_batch), ("skew50m", run_skew)):
+            t0 = time.perf_counter()
+            try:
+                other[name] = fn(args, local, K=args.form_steps, W=3)
+            except Exception as e:  # reported in the line; the headline does not depend on it
+                other[name] = {"error": f"{type(e).__name__}: {e}"}
+            other[name]["wall_s"] = time.perf_counter() - t0
     head = forms[modes[0]]
     parity = {}
     if len(modes) == 2:
@@ -1160,8 +1180,14 @@ def main():
                 "roofline": roofline(head, N, args.buckets, modes[0]), "clocks": head["clocks"], "e2e": head["e2e"],
                 "cpu_baseline": cpu, "parity": parity,
                 "gpu_launches": head["gpu_launches"], "serving": serve, "compaction": compact,
-                "forms": {m: {k: v for k, v in f.items()} for m, f in forms.items()}}
+                "forms": dict({m: {k: v for k, v in f.items()} for m, f in forms.items()}, **other)}
+        bad = {k: v["mismatching_steps"] for k, v in parity.items() if v.get("mismatching_steps")}
+        line["parity_ok"] = not bad
         print(json.dumps(line), flush=True)
+        if bad:
+            # the line above carries the numbers; a run whose meetings differ fails
+            print(f"meetings differ on steps {bad}", file=sys.stderr)
+            sys.exit(3)
 
 
 if __name__ == "__main__":

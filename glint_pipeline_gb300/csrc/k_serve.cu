@@ -48,6 +48,7 @@ struct HopArgs {
     uint32_t *counts;                      /* [slot] next-list sizes */
     unsigned long long *scanned;           /* [slot] keys read */
     const uint32_t *active;                /* [A] slots taking part in this launch */
+    const uint32_t *front;                 /* [A] their frontier sizes */
     const unsigned long long *prefix;      /* [A + 1] their items (frontier x blocks), prefix sums */
     const uint32_t *rel;                   /* each active slot's blocks, concatenated */
     const uint32_t *rel_off;               /* [A + 1] where each active slot's blocks start in rel */
@@ -58,15 +59,19 @@ struct HopArgs {
  * when it is new; the lanes that call together and append to the same slot
  * take their places with one atomic (a slot's counter is one address that
  * every new object of a large frontier would otherwise hit) */
-__device__ inline void visit(const HopArgs &a, uint32_t s, uint32_t next_list, uint32_t target) {
+__device__ inline uint32_t visited_word(const HopArgs &a, uint32_t s, uint32_t target) {
+    return target < a.N ? __ldcg(&a.visited[(size_t)s * a.words + (target >> 5)]) : ~0u;
+}
+
+/* as visit, with the target's bitmap word already read (visited_word) */
+__device__ inline void visit_seen(const HopArgs &a, uint32_t s, uint32_t next_list, uint32_t target, uint32_t seen) {
     const unsigned calling = __activemask();
     bool fresh = false;
     if (target < a.N) {
         /* a query's bits only go from 0 to 1, so a set bit read from L2 is
          * final and saves the atomic; a clear one is settled by the atomic */
         const uint32_t bit = 1u << (target & 31);
-        uint32_t *w = &a.visited[(size_t)s * a.words + (target >> 5)];
-        if (!(__ldcg(w) & bit)) fresh = !(atomicOr(w, bit) & bit);
+        if (!(seen & bit)) fresh = !(atomicOr(&a.visited[(size_t)s * a.words + (target >> 5)], bit) & bit);
     }
     const unsigned appending = __ballot_sync(calling, fresh);
     if (!fresh) return;
@@ -79,73 +84,197 @@ __device__ inline void visit(const HopArgs &a, uint32_t s, uint32_t next_list, u
     if (idx < a.N) a.lists[((size_t)s * 2 + next_list) * a.N + idx] = target;
 }
 
-__global__ void __launch_bounds__(256) k_serve_hop(HopArgs a) {
-    const unsigned long long total = a.prefix[a.A];
-    /* keys read, per slot: summed here while this thread's items stay in one
-     * slot (slots own contiguous item ranges), added once when they move on */
-    uint32_t acc_slot = 0xffffffffu;
-    unsigned long long acc = 0;
-    for (unsigned long long it = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; it < total;
-         it += (unsigned long long)gridDim.x * blockDim.x) {
-        uint32_t lo = 0, hi = a.A; /* prefix[lo] <= it < prefix[lo + 1] */
-        while (hi - lo > 1) {
-            const uint32_t mid = (lo + hi) / 2;
-            if (a.prefix[mid] <= it) lo = mid;
-            else hi = mid;
-        }
-        /* block-major within a slot: consecutive items take consecutive
-         * frontier objects (ascending ids) of one block, whose sids,
-         * key ranges and keys then lie close together */
-        const uint32_t nrel = a.rel_off[lo + 1] - a.rel_off[lo];
-        const unsigned long long fr = (a.prefix[lo + 1] - a.prefix[lo]) / nrel;
-        const unsigned long long local = it - a.prefix[lo];
-        const unsigned long long bi = local / fr;
-        const unsigned long long f = local - bi * fr;
-        const uint32_t b = a.rel[a.rel_off[lo] + (uint32_t)bi];
-        const uint32_t s = a.active[lo];
-        const SlotParam sp = a.param[s];
-        const uint32_t obj = a.lists[((size_t)s * 2 + sp.cur) * a.N + f];
-        const StoreBlockDev blk = a.blocks[b];
-        const uint32_t sid = blk.sids[obj];
-        if (sid == 0) continue;
-        const uint32_t n = blk.count[obj], first = blk.first[obj];
-        const uint32_t nl = sp.cur ^ 1u;
-        if (s != acc_slot) {
-            if (acc) atomicAdd(&a.scanned[acc_slot], acc);
-            acc_slot = s;
-            acc = 0;
-        }
-        acc += n;
-        if (sid == 1) {
-            for (uint32_t j = 0; j < n; ++j) {
-                const ulonglong2 k = blk.okeys[first + j];
-                const uint32_t end = (uint32_t)k.x + blk.end_time_min, duration = (uint32_t)(k.x >> 32);
-                const uint32_t start = end - duration;
-                if (sp.window && !(start < sp.t_end && sp.t_start < end)) continue;
-                visit(a, s, nl, (uint32_t)k.y & ((1u << 26) - 1));
-            }
-            continue;
-        }
-        const uint32_t c = sid - 2;
-        if (c >= blk.C) continue;
-        const glint_ctf_meta m = blk.ctfs[c];
-        const uint32_t kb = m.key_bit / 8;
-        const uint8_t *base = blk.keys + blk.byte_index[c] + (unsigned long long)(first - blk.key_index[c]) * kb;
-        for (uint32_t j = 0; j < n; ++j) {
-            const uint8_t *p = base + (size_t)j * kb;
-            unsigned __int128 v = load_key(p, kb, blk.keys + blk.key_bytes);
-            v >>= m.mbr_bit;
-            const uint32_t end = (uint32_t)(v & ((1ull << m.end_bit) - 1)) + blk.end_time_min;
-            v >>= m.end_bit;
-            const uint32_t duration = (uint32_t)(v & ((1ull << m.duration_bit) - 1));
-            v >>= m.duration_bit;
-            const uint32_t target = (uint32_t)(v & ((1ull << m.id_bit) - 1));
-            const uint32_t start = end - duration;
-            if (sp.window && !(start < sp.t_end && sp.t_start < end)) continue;
-            visit(a, s, nl, target);
-        }
+__device__ inline void visit(const HopArgs &a, uint32_t s, uint32_t next_list, uint32_t target) {
+    visit_seen(a, s, next_list, target, visited_word(a, s, target));
+}
+
+/* one item's keys as the hop reads them: where they start, how many, and
+ * how a key decodes (kind 1: the oversize buffer's 16-byte keys; kind 2: a
+ * CTF's packed keys, whose end, duration and target fields lie in the 64
+ * bits from byte off of the key when fast is set) */
+struct HopItem {
+    const uint8_t *base;
+    const uint8_t *end;      /* the end of the block's packed keys */
+    uint32_t n, s, nl, kind;
+    uint32_t kb, off, fast, mbr_bit;
+    uint32_t end_bit, dur_bit, end_mask, dur_mask;
+    uint32_t id_mask, etm, window, t_start;
+    uint32_t t_end, pad0, pad1, pad2;
+};
+
+constexpr int kHopThreads = 256;
+constexpr int kHopKeys = 4; /* keys per lane per round */
+
+/* the 64 bits at p, which need not be aligned; whole words while they stay
+ * inside the buffer ending at `end` (whose start is 8-aligned) */
+__device__ inline unsigned long long load_u64(const uint8_t *p, const uint8_t *end) {
+    const uintptr_t a = (uintptr_t)p;
+    const uint64_t *w = (const uint64_t *)(a & ~(uintptr_t)7);
+    const uint32_t sh = (uint32_t)(a & 7) * 8;
+    if ((const uint8_t *)(w + 2) <= end) {
+        const uint64_t lo = w[0];
+        return sh ? (lo >> sh) | (w[1] << (64 - sh)) : lo;
     }
-    if (acc) atomicAdd(&a.scanned[acc_slot], acc);
+    unsigned long long v = 0;
+    for (uint32_t i = 0; i < 8 && p + i < end; ++i) v |= (unsigned long long)p[i] << (8 * i);
+    return v;
+}
+
+/* Each warp takes 32 consecutive items, one per lane, and looks up the
+ * object's sid, first key and key count in the item's block.  An object has
+ * anywhere from none to hundreds of keys in a block, so the warp then walks
+ * the keys of all 32 items together, 32 at a time: lane l takes the warp's
+ * key k0 + l, finds its item by a binary search over the items' key counts'
+ * prefix sums, and reads that item's decoding from shared memory.  Every lane
+ * has a key on every round but the last, and the warp's loop count is its
+ * total keys / 32 instead of its largest item's key count.  A lane decodes
+ * kHopKeys keys before it reads their bitmap words, so that their loads
+ * overlap. */
+__global__ void __launch_bounds__(kHopThreads) k_serve_hop(HopArgs a) {
+    __shared__ HopItem items[kHopThreads];
+    __shared__ uint32_t koff[kHopThreads];
+    const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+    HopItem *wi = items + wib * 32;
+    uint32_t *wo = koff + wib * 32;
+    const unsigned long long total = a.prefix[a.A];
+    const unsigned long long warps = (unsigned long long)gridDim.x * (kHopThreads / 32);
+    for (unsigned long long w = blockIdx.x * (unsigned long long)(kHopThreads / 32) + wib; w * 32 < total;
+         w += warps) {
+        const unsigned long long it = w * 32 + lane;
+        HopItem h;
+        h.n = 0;
+        h.kind = 0;
+        h.s = 0;
+        if (it < total) {
+            uint32_t lo = 0, hi = a.A; /* prefix[lo] <= it < prefix[lo + 1] */
+            while (hi - lo > 1) {
+                const uint32_t mid = (lo + hi) / 2;
+                if (a.prefix[mid] <= it) lo = mid;
+                else hi = mid;
+            }
+            /* block-major within a slot: consecutive items take consecutive
+             * frontier objects (ascending ids) of one block, whose sids,
+             * key ranges and keys then lie close together */
+            const uint32_t fr = a.front[lo];
+            const unsigned long long local = it - a.prefix[lo];
+            uint32_t bi, f;
+            if (local < (1ull << 32)) {
+                bi = (uint32_t)local / fr;
+                f = (uint32_t)local - bi * fr;
+            } else {
+                bi = (uint32_t)(local / fr);
+                f = (uint32_t)(local - (unsigned long long)bi * fr);
+            }
+            const uint32_t b = a.rel[a.rel_off[lo] + bi];
+            const uint32_t s = a.active[lo];
+            const SlotParam sp = a.param[s];
+            const uint32_t obj = a.lists[((size_t)s * 2 + sp.cur) * a.N + f];
+            const StoreBlockDev &blk = a.blocks[b];
+            const uint32_t sid = blk.sids[obj];
+            h.s = s;
+            h.nl = sp.cur ^ 1u;
+            h.window = sp.window;
+            h.t_start = sp.t_start;
+            h.t_end = sp.t_end;
+            h.etm = blk.end_time_min;
+            if (sid == 1) {
+                h.n = blk.count[obj];
+                h.kind = 1;
+                h.base = reinterpret_cast<const uint8_t *>(blk.okeys + blk.first[obj]);
+            } else if (sid >= 2 && sid - 2 < blk.C) {
+                const uint32_t c = sid - 2;
+                const glint_ctf_meta &m = blk.ctfs[c];
+                const uint32_t kb = m.key_bit / 8, mb = m.mbr_bit, eb = m.end_bit, db = m.duration_bit,
+                               ib = m.id_bit;
+                h.n = blk.count[obj];
+                h.kind = 2;
+                h.kb = kb;
+                h.mbr_bit = mb;
+                h.off = mb / 8;
+                h.fast = (mb & 7) + eb + db + ib <= 64;
+                h.end_bit = eb;
+                h.dur_bit = db;
+                h.end_mask = eb >= 32 ? 0xffffffffu : (1u << eb) - 1u;
+                h.dur_mask = db >= 32 ? 0xffffffffu : (1u << db) - 1u;
+                h.id_mask = ib >= 32 ? 0xffffffffu : (1u << ib) - 1u;
+                h.end = blk.keys + blk.key_bytes;
+                h.base = blk.keys + blk.byte_index[c] + (unsigned long long)(blk.first[obj] - blk.key_index[c]) * kb;
+            }
+        }
+        /* keys read, per slot: the lanes of one slot add with one reduction */
+        const unsigned withkeys = __ballot_sync(0xffffffffu, h.n != 0);
+        if (h.n) {
+            const unsigned peers = __match_any_sync(withkeys, h.s);
+            const uint32_t grp = __reduce_add_sync(peers, h.n);
+            if (lane == __ffs(peers) - 1) atomicAdd(&a.scanned[h.s], (unsigned long long)grp);
+        }
+        /* exclusive prefix of the key counts over the warp */
+        uint32_t incl = h.n;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const uint32_t T = __shfl_sync(0xffffffffu, incl, 31);
+        wi[lane] = h;
+        wo[lane] = incl - h.n;
+        __syncwarp();
+        /* kHopKeys keys per lane in flight: their loads, then their bitmap
+         * words, then the (rare) atomics and appends */
+        for (uint32_t k0 = 0; k0 < T; k0 += 32 * kHopKeys) {
+            uint32_t tg[kHopKeys], sl[kHopKeys], nx[kHopKeys], seen[kHopKeys];
+#pragma unroll
+            for (int u = 0; u < kHopKeys; ++u) {
+                const uint32_t k = k0 + u * 32 + lane;
+                tg[u] = 0xffffffffu;
+                sl[u] = 0;
+                nx[u] = 0;
+                if (k < T) {
+                    /* the last item whose first key is at or before k: it has
+                     * keys, since an item without keys shares its offset with
+                     * the item after it, and k < T rules out the last lane */
+                    uint32_t lo = 0;
+#pragma unroll
+                    for (uint32_t step = 16; step; step >>= 1)
+                        if (lo + step < 32 && wo[lo + step] <= k) lo += step;
+                    const HopItem &x = wi[lo];
+                    const uint32_t j = k - wo[lo];
+                    sl[u] = x.s;
+                    nx[u] = x.nl;
+                    uint32_t end, duration, t;
+                    if (x.kind == 2 && x.fast) {
+                        /* end, duration and target from one 64-bit window */
+                        unsigned long long v = load_u64(x.base + (size_t)j * x.kb + x.off, x.end);
+                        v >>= x.mbr_bit & 7;
+                        end = ((uint32_t)v & x.end_mask) + x.etm;
+                        v >>= x.end_bit;
+                        duration = (uint32_t)v & x.dur_mask;
+                        v >>= x.dur_bit;
+                        t = (uint32_t)v & x.id_mask;
+                    } else if (x.kind == 2) {
+                        unsigned __int128 v = load_key(x.base + (size_t)j * x.kb, x.kb, x.end);
+                        v >>= x.mbr_bit;
+                        end = (uint32_t)(v & ((1ull << x.end_bit) - 1)) + x.etm;
+                        v >>= x.end_bit;
+                        duration = (uint32_t)(v & ((1ull << x.dur_bit) - 1));
+                        v >>= x.dur_bit;
+                        t = (uint32_t)v & x.id_mask;
+                    } else {
+                        const ulonglong2 kk = reinterpret_cast<const ulonglong2 *>(x.base)[j];
+                        end = (uint32_t)kk.x + x.etm;
+                        duration = (uint32_t)(kk.x >> 32);
+                        t = (uint32_t)kk.y & ((1u << 26) - 1);
+                    }
+                    const uint32_t start = end - duration;
+                    if (!x.window || (start < x.t_end && x.t_start < end)) tg[u] = t;
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kHopKeys; ++u) seen[u] = visited_word(a, sl[u], tg[u]);
+#pragma unroll
+            for (int u = 0; u < kHopKeys; ++u) visit_seen(a, sl[u], nx[u], tg[u], seen[u]);
+        }
+        __syncwarp();
+    }
 }
 
 /* the new ids of the active slots as (slot rank, id) keys: slot rank r's
@@ -228,6 +357,7 @@ struct glint_server {
     uint32_t *visited = nullptr, *lists = nullptr, *counts = nullptr, *active = nullptr, *seed_slots = nullptr;
     SlotParam *param = nullptr;
     unsigned long long *scanned = nullptr, *prefix = nullptr, *sprefix = nullptr;
+    uint32_t *front = nullptr;
     uint32_t *seeds = nullptr;
     uint64_t seeds_cap = 0;
     StoreBlockDev *blocks = nullptr;
@@ -250,7 +380,7 @@ struct glint_server {
 static void server_release(glint_server *v) {
     void *ps[] = {v->visited, v->lists, v->counts, v->active, v->seed_slots, v->param, v->scanned, v->prefix,
                   v->sprefix, v->seeds, v->blocks, v->rk, v->rk2, v->roff, v->rv, v->rv2, v->rids, v->rs_tmp,
-                  v->rscan, v->rel, v->rel_off};
+                  v->rscan, v->rel, v->rel_off, v->front};
     for (void *p : ps)
         if (p) cudaFree(p);
 }
@@ -305,6 +435,7 @@ extern "C" glint_status glint_server_create(glint_ctx *c, uint32_t max_slots, gl
     A((void **)&v->param, sizeof(SlotParam) * S);
     A((void **)&v->scanned, sizeof(unsigned long long) * S);
     A((void **)&v->prefix, sizeof(unsigned long long) * (S + 1));
+    A((void **)&v->front, sizeof(uint32_t) * S);
     A((void **)&v->sprefix, sizeof(unsigned long long) * (S + 1));
     if (e != cudaSuccess) {
         server_release(v);
@@ -369,6 +500,7 @@ static HopArgs server_args(glint_server *v, uint32_t nb) {
     a.scanned = v->scanned;
     a.active = v->active;
     a.prefix = v->prefix;
+    a.front = v->front;
     a.rel = v->rel;
     a.rel_off = v->rel_off;
     a.A = 0;
@@ -454,13 +586,14 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
      * key inside its window: a key of a block ends at most at end_time_max
      * and starts no earlier than start_min, and it counts when
      * start < t_end and t_start < end */
-    std::vector<uint32_t> act, rel;
+    std::vector<uint32_t> act, rel, front;
     std::vector<uint32_t> rel_off(1, 0);
     std::vector<unsigned long long> prefix(1, 0);
     for (uint32_t k = 0; k < v->slots; ++k) {
         const SlotState &st = v->state[k];
         if (!st.busy || st.hop >= st.hops) continue;
         act.push_back(k);
+        front.push_back(st.frontier);
         const SlotParam &sp = v->hparam[k];
         uint32_t nrel = 0;
         for (uint32_t i = 0; i < nb; ++i) {
@@ -493,6 +626,7 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
         a.rel_off = v->rel_off;
         cudaMemcpyAsync(v->param, v->hparam.data(), sizeof(SlotParam) * v->slots, cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(v->active, act.data(), sizeof(uint32_t) * act.size(), cudaMemcpyHostToDevice, s);
+        cudaMemcpyAsync(v->front, front.data(), sizeof(uint32_t) * front.size(), cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(v->prefix, prefix.data(), sizeof(unsigned long long) * prefix.size(), cudaMemcpyHostToDevice,
                         s);
         if (!rel.empty())
@@ -501,7 +635,7 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
         for (uint32_t k : act) cudaMemsetAsync(v->counts + k, 0, sizeof(uint32_t), s);
         a.A = (uint32_t)act.size();
         const unsigned long long items = prefix.back();
-        if (items) k_serve_hop<<<grid_for(items, 256, 152u * 16u), 256, 0, s>>>(a);
+        if (items) k_serve_hop<<<grid_for((items + 31) / 32, kHopThreads / 32, 152u * 8u), kHopThreads, 0, s>>>(a);
         std::vector<uint32_t> cnt(v->slots);
         std::vector<unsigned long long> scanned(v->slots);
         cudaMemcpyAsync(cnt.data(), v->counts, sizeof(uint32_t) * v->slots, cudaMemcpyDeviceToHost, s);
@@ -606,7 +740,7 @@ void servers_detach(glint_ctx *c) {
         v->param = nullptr;
         v->scanned = v->prefix = v->sprefix = nullptr;
         v->blocks = nullptr;
-        v->rel = v->rel_off = nullptr;
+        v->rel = v->rel_off = v->front = nullptr;
         v->ctx = nullptr;
     }
     c->servers.clear();

@@ -14,7 +14,9 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_SO = os.path.join(HERE, "liboracle.so")
-REF_SO = os.path.join(HERE, "_ref", "libglintref.so")
+# GLINT_REF_SO selects another build of the reference's CPU stages (e.g. the
+# as-shipped flags, build_ref.sh REF_OPT/REF_LIB)
+REF_SO = os.environ.get("GLINT_REF_SO") or os.path.join(HERE, "_ref", "libglintref.so")
 # the reference checkout: GLINT_REFERENCE_ROOT, else a directory named
 # "reference" beside this repository
 REFERENCE_ROOT = os.environ.get("GLINT_REFERENCE_ROOT") or os.path.join(os.path.dirname(os.path.dirname(HERE)),
