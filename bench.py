@@ -66,7 +66,8 @@ def parse():
                         "compared with the GPU's on all of them)")
     p.add_argument("--cpu-warmup", type=int, default=1)
     p.add_argument("--cpu-threads", type=int, default=0, help="0: all host cores")
-    p.add_argument("--serve-seconds", type=float, default=6.0)
+    p.add_argument("--serve-seconds", type=float, default=6.0,
+                   help="Poisson stream length; 0 serves only the 2-hop queries from 1000 seeds")
     p.add_argument("--serve-rate", type=float, default=200.0)
     p.add_argument("--serve-sweep", default="50,2000",
                    help="further Poisson rates (req/s) served for --serve-seconds / 2 each; empty: none")
@@ -84,9 +85,12 @@ def parse():
                    help="split_num of the compaction leg (the reference tool merges into 56^2 = 3136 CTFs)")
     p.add_argument("--compact-sample-objects", type=int, default=500_000)
     p.add_argument("--no-compact", action="store_true")
-    p.add_argument("--workload", default="step10m", choices=["step10m", "batch64", "skew50m", "compact"],
+    p.add_argument("--workload", default="step10m", choices=["step10m", "batch64", "skew50m", "compact", "serve"],
                    help="step10m: the headline line; batch64 / skew50m: the batching and precision forms; "
-                        "compact: the compaction sample alone (--compact-sample-objects objects)")
+                        "compact: the compaction sample alone (--compact-sample-objects objects); serve: the "
+                        "serving leg alone (store build over --serve-steps, then the queries)")
+    p.add_argument("--serve-kv", type=int, default=0,
+                   help="keys pending before the serving store's build flushes a block; 0: the default 2^26")
     p.add_argument("--regions", type=int, default=64)
     p.add_argument("--form-steps", type=int, default=6,
                    help="timed steps of the batching and skew legs inside the default run (their own "
@@ -598,8 +602,12 @@ def serving(args, bench, N, t_hi, sweep_rates=True):
     rng = np.random.default_rng(0x474C494E54000005)
     dl = args.serve_deadline
     srv = gp.Server(bench, max_slots=64)
-    lat, wall, reached, n, unf = poisson_stream(srv, rng, N, t_hi, args.serve_rate, args.serve_seconds, dl)
-    main = latency_summary(lat, n, unf, dl)
+    if args.serve_seconds > 0:
+        lat, wall, reached, n, unf = poisson_stream(srv, rng, N, t_hi, args.serve_rate, args.serve_seconds, dl)
+        main = latency_summary(lat, n, unf, dl)
+    else:
+        wall, reached, n, unf, main = 1.0, 0, 0, 0, {}
+        sweep_rates = False
     sweep = {}
     rates = [float(x) for x in args.serve_sweep.split(",") if x.strip() and sweep_rates]
     left = unf
@@ -666,7 +674,8 @@ def serving_store(args, local, N, pb, ob, box, first):
     keep = max(1, int(dev_budget // block_bytes))
     host_keep = max(0, int(host_budget // block_bytes))
     cfg = gp.Configuration(num_objects=N, num_meeting_buckets=args.buckets, device=local, precision_mode=1,
-                           auto_flush=True, store_keep=keep, store_host_keep=host_keep)
+                           auto_flush=True, store_keep=keep, store_host_keep=host_keep,
+                           kv_restriction=args.serve_kv)
     bench = gp.DeviceBench(cfg, box, first)
     gh = ctypes.c_void_p()
     assert lib.glint_gen_create(pb, len(pb), ob, N, len(ob) // N, 0, ctypes.byref(gh)) == 0
@@ -1093,6 +1102,19 @@ def main():
     if args.workload == "skew50m":
         if rank == 0:
             print(json.dumps(run_skew(args, local)), flush=True)
+        return
+    if args.workload == "serve":
+        if rank == 0:
+            from glint_pipeline_gb300.tracegen import SEED_SCALE, TraceGenerator
+            g = TraceGenerator(SEED_SCALE, args.objects)
+            box, first = g.box(), g.steps(1)[0]
+            g.close()
+            g2 = TraceGenerator(SEED_SCALE, args.objects)
+            pb, ob = g2.params_bytes(), g2.objects_bytes()
+            g2.close()
+            res = serving_store(args, local, args.objects, pb, ob, box, first)
+            print(json.dumps({"workload": "serve", "metric": "query latency over a store of --serve-steps steps",
+                              "serving": res}), flush=True)
         return
     if args.workload == "compact":
         if rank == 0:
