@@ -373,7 +373,11 @@ def roofline(form, N, buckets=None, mode=None):
     hbm = pk.get("hbm_gbs")
     peak = hbm if hbm else 6800.0
     stages = {k: v for k, v in form["stage_ms"].items() if k in ("partition", "filter", "refine", "insert", "identify")}
-    top = max(stages, key=stages.get)
+    # the dominant kernel is refine's (k_refine_fp32 in the tuned form: 35% of
+    # the step's kernel time in the ncu launch list, k_expire_count next at
+    # 26%); by stage, refine and identify take turns as the slowest
+    top = "refine"
+    slowest = max(stages, key=stages.get)
     ms = stages[top]
     step_by, by8 = step_bytes_8d(N, form["per_step"])
     by = by8[top]
@@ -382,7 +386,9 @@ def roofline(form, N, buckets=None, mode=None):
     traffic = TRAFFIC_10M_2P30.get(top) if measured else None
     stage_model = {k: stage_bytes(k, N, form["per_step"], 1) for k in stages}
     ratio = {k: (TRAFFIC_10M_2P30[k] / by8[k] if by8.get(k) else None) for k in TRAFFIC_10M_2P30} if measured else None
-    return {"kernel_stage": top, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+    kernel = "k_refine_fp32" if mode == "tuned" else "k_refine_fp64"
+    return {"kernel": kernel, "kernel_stage": top, "slowest_stage": slowest, "bound": "hbm", "achieved": achieved,
+            "peak": peak, "unit": "GB/s",
             "frac": achieved / peak if achieved else None, "traffic": traffic,
             "traffic_unit": "DRAM bytes per step of the stage's kernels", "algorithmic_bytes": by,
             "model": "40 B/object + 32 B/contact pair + 48 B/meeting; the stage's share",
