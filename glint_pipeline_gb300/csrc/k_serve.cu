@@ -277,6 +277,137 @@ __global__ void __launch_bounds__(kHopThreads) k_serve_hop(HopArgs a) {
     }
 }
 
+/* ---- pull hops -----------------------------------------------------------
+ * When a slot's frontier is at least as large as the set of objects it has
+ * not reached, the hop runs from the other side: every unreached object u
+ * reads its own keys in the window's blocks and is reached when one of its
+ * targets was reached before this hop.  A meeting's two keys (a -> b and
+ * b -> a, cuda/geometry.cu:714-734) lie in the same block with the same
+ * times, so u has a key to a reached object v exactly when v has one to u;
+ * and v was reached at the previous hop, since a v reached earlier would have
+ * reached u already.  The reached set is read as it stood before the hop
+ * (its bits are set after it, k_serve_mark), so the hop's result is the one
+ * the frontier's own walk gives, and u stops at its first such key. */
+
+/* the unreached objects of pull slot blockIdx.y into its frontier list,
+ * ascending within each warp's 1024 ids */
+__global__ void __launch_bounds__(256) k_serve_unvisited(HopArgs b, unsigned int *ucount) {
+    const uint32_t s = b.active[blockIdx.y];
+    const uint32_t *vis = b.visited + (size_t)s * b.words;
+    uint32_t *out = b.lists + ((size_t)s * 2 + b.param[s].cur) * b.N;
+    const int lane = threadIdx.x & 31;
+    const uint32_t nw = (b.N + 31) / 32;
+    for (uint32_t w0 = blockIdx.x * blockDim.x; w0 < nw; w0 += gridDim.x * blockDim.x) {
+        const uint32_t w = w0 + threadIdx.x;
+        uint32_t inv = 0;
+        if (w < nw) {
+            inv = ~vis[w];
+            if (w == nw - 1 && (b.N & 31)) inv &= (1u << (b.N & 31)) - 1u;
+        }
+        const uint32_t k = __popc(inv);
+        uint32_t incl = k;
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        uint32_t base = 0;
+        if (lane == 31 && incl) base = atomicAdd(&ucount[s], incl);
+        base = __shfl_sync(0xffffffffu, base, 31);
+        uint32_t at = base + incl - k;
+        while (inv) {
+            const int bit = __ffs(inv) - 1;
+            inv &= inv - 1u;
+            if (at < b.N) out[at] = w * 32 + (uint32_t)bit;
+            ++at;
+        }
+    }
+}
+
+/* one warp per unreached object: its keys in the slot's blocks, 32 blocks
+ * at a time, until one reaches an object reached before this hop */
+__global__ void __launch_bounds__(256) k_serve_pull(HopArgs b) {
+    const int lane = threadIdx.x & 31;
+    const unsigned long long total = b.prefix[b.A];
+    const unsigned long long nwarps = (unsigned long long)gridDim.x * (blockDim.x / 32);
+    for (unsigned long long w = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) / 32; w < total;
+         w += nwarps) {
+        uint32_t lo = 0, hi = b.A; /* prefix[lo] <= w < prefix[lo + 1] */
+        while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) / 2;
+            if (b.prefix[mid] <= w) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t s = b.active[lo];
+        const SlotParam sp = b.param[s];
+        const uint32_t u = b.lists[((size_t)s * 2 + sp.cur) * b.N + (w - b.prefix[lo])];
+        const uint32_t *vis = b.visited + (size_t)s * b.words;
+        const uint32_t r0 = b.rel_off[lo], nrel = b.rel_off[lo + 1] - r0;
+        bool found = false;
+        unsigned long long keys = 0;
+        for (uint32_t r = 0; r < nrel && !found; r += 32) {
+            bool hit = false;
+            if (r + lane < nrel) {
+                const StoreBlockDev &blk = b.blocks[b.rel[r0 + r + lane]];
+                const uint32_t sid = blk.sids[u];
+                uint32_t n = 0;
+                if (sid == 1) {
+                    n = blk.count[u];
+                    const ulonglong2 *k = blk.okeys + blk.first[u];
+                    for (uint32_t j = 0; j < n && !hit; ++j) {
+                        const ulonglong2 kk = k[j];
+                        const uint32_t end = (uint32_t)kk.x + blk.end_time_min, dur = (uint32_t)(kk.x >> 32);
+                        const uint32_t t = (uint32_t)kk.y & ((1u << 26) - 1);
+                        ++keys;
+                        if (sp.window && !((end - dur) < sp.t_end && sp.t_start < end)) continue;
+                        if (t < b.N && ((vis[t >> 5] >> (t & 31)) & 1u)) hit = true;
+                    }
+                } else if (sid >= 2 && sid - 2 < blk.C) {
+                    const uint32_t c = sid - 2;
+                    const glint_ctf_meta &m = blk.ctfs[c];
+                    const uint32_t kb = m.key_bit / 8;
+                    n = blk.count[u];
+                    const uint8_t *base =
+                        blk.keys + blk.byte_index[c] + (unsigned long long)(blk.first[u] - blk.key_index[c]) * kb;
+                    const uint8_t *kend = blk.keys + blk.key_bytes;
+                    for (uint32_t j = 0; j < n && !hit; ++j) {
+                        unsigned __int128 v = load_key(base + (size_t)j * kb, kb, kend);
+                        v >>= m.mbr_bit;
+                        const uint32_t end = (uint32_t)(v & ((1ull << m.end_bit) - 1)) + blk.end_time_min;
+                        v >>= m.end_bit;
+                        const uint32_t dur = (uint32_t)(v & ((1ull << m.duration_bit) - 1));
+                        v >>= m.duration_bit;
+                        const uint32_t t = (uint32_t)(v & ((1ull << m.id_bit) - 1));
+                        ++keys;
+                        if (sp.window && !((end - dur) < sp.t_end && sp.t_start < end)) continue;
+                        if (t < b.N && ((vis[t >> 5] >> (t & 31)) & 1u)) hit = true;
+                    }
+                }
+            }
+            found = __any_sync(0xffffffffu, hit);
+        }
+        for (int o = 16; o > 0; o >>= 1) keys += __shfl_down_sync(0xffffffffu, keys, o);
+        if (lane == 0) {
+            if (keys) atomicAdd(&b.scanned[s], keys);
+            if (found) {
+                const uint32_t idx = atomicAdd(&b.counts[s], 1u);
+                if (idx < b.N) b.lists[((size_t)s * 2 + (sp.cur ^ 1u)) * b.N + idx] = u;
+            }
+        }
+    }
+}
+
+/* the objects a pull hop reached join the reached set of pull slot blockIdx.y */
+__global__ void k_serve_mark(HopArgs b) {
+    const uint32_t s = b.active[blockIdx.y];
+    const uint32_t n = min(b.counts[s], b.N);
+    const uint32_t *next = b.lists + ((size_t)s * 2 + (b.param[s].cur ^ 1u)) * b.N;
+    uint32_t *vis = b.visited + (size_t)s * b.words;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t u = next[i];
+        atomicOr(&vis[u >> 5], 1u << (u & 31));
+    }
+}
+
 /* the new ids of the active slots as (slot rank, id) keys: slot rank r's
  * count[r] ids start at off[r] */
 __global__ void k_serve_collect(const uint32_t *__restrict__ lists, uint32_t N, const uint32_t *__restrict__ act,
@@ -340,6 +471,7 @@ struct SlotState {
     bool busy = false;
     uint64_t ticket = 0;
     uint32_t hops = 0, hop = 0, cur = 0, frontier = 0;
+    uint64_t reached = 0; /* seeds and every hop's new objects so far */
     std::vector<uint32_t> ids;
     uint64_t hop_end[kMaxHops] = {};
 };
@@ -358,6 +490,8 @@ struct glint_server {
     SlotParam *param = nullptr;
     unsigned long long *scanned = nullptr, *prefix = nullptr, *sprefix = nullptr;
     uint32_t *front = nullptr;
+    unsigned long long *pprefix = nullptr; /* pull slots' items (their unreached objects), prefix sums */
+    unsigned int *ucount = nullptr;        /* [slot] unreached objects listed */
     uint32_t *seeds = nullptr;
     uint64_t seeds_cap = 0;
     StoreBlockDev *blocks = nullptr;
@@ -380,7 +514,7 @@ struct glint_server {
 static void server_release(glint_server *v) {
     void *ps[] = {v->visited, v->lists, v->counts, v->active, v->seed_slots, v->param, v->scanned, v->prefix,
                   v->sprefix, v->seeds, v->blocks, v->rk, v->rk2, v->roff, v->rv, v->rv2, v->rids, v->rs_tmp,
-                  v->rscan, v->rel, v->rel_off, v->front};
+                  v->rscan, v->rel, v->rel_off, v->front, v->pprefix, v->ucount};
     for (void *p : ps)
         if (p) cudaFree(p);
 }
@@ -436,6 +570,8 @@ extern "C" glint_status glint_server_create(glint_ctx *c, uint32_t max_slots, gl
     A((void **)&v->scanned, sizeof(unsigned long long) * S);
     A((void **)&v->prefix, sizeof(unsigned long long) * (S + 1));
     A((void **)&v->front, sizeof(uint32_t) * S);
+    A((void **)&v->pprefix, sizeof(unsigned long long) * (S + 1));
+    A((void **)&v->ucount, sizeof(unsigned int) * S);
     A((void **)&v->sprefix, sizeof(unsigned long long) * (S + 1));
     if (e != cudaSuccess) {
         server_release(v);
@@ -579,7 +715,7 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
         std::vector<uint32_t> cnt(v->slots);
         cudaMemcpyAsync(cnt.data(), v->counts, sizeof(uint32_t) * v->slots, cudaMemcpyDeviceToHost, s);
         if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return server_fail(v, e, "seed");
-        for (uint32_t k : admitted) v->state[k].frontier = cnt[k];
+        for (uint32_t k : admitted) v->state[k].frontier = v->state[k].reached = cnt[k];
     }
 
     /* one hop for every active slot, over the kept blocks that can hold a
@@ -588,10 +724,21 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
      * start < t_end and t_start < end */
     std::vector<uint32_t> act, rel, front;
     std::vector<uint32_t> rel_off(1, 0);
-    std::vector<unsigned long long> prefix(1, 0);
-    for (uint32_t k = 0; k < v->slots; ++k) {
+    std::vector<unsigned long long> prefix(1, 0), pprefix(1, 0);
+    /* frontier walks first, then the pull slots (their frontier reaches at
+     * least as many objects as are left) */
+    std::vector<uint32_t> order;
+    for (int pass = 0; pass < 2; ++pass)
+        for (uint32_t k = 0; k < v->slots; ++k) {
+            const SlotState &st = v->state[k];
+            if (!st.busy || st.hop >= st.hops) continue;
+            const bool pull = (uint64_t)st.frontier >= (uint64_t)N - st.reached;
+            if (pull == (pass == 1)) order.push_back(k);
+        }
+    uint32_t n_push = 0;
+    for (uint32_t k : order) {
         const SlotState &st = v->state[k];
-        if (!st.busy || st.hop >= st.hops) continue;
+        const bool pull = (uint64_t)st.frontier >= (uint64_t)N - st.reached;
         act.push_back(k);
         front.push_back(st.frontier);
         const SlotParam &sp = v->hparam[k];
@@ -603,7 +750,12 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
             ++nrel;
         }
         rel_off.push_back((uint32_t)rel.size());
-        prefix.push_back(prefix.back() + (unsigned long long)st.frontier * nrel);
+        if (pull) {
+            pprefix.push_back(pprefix.back() + ((uint64_t)N - st.reached));
+        } else {
+            prefix.push_back(prefix.back() + (unsigned long long)st.frontier * nrel);
+            ++n_push;
+        }
     }
     if (!act.empty()) {
         if (v->rel_cap < rel.size() + 1) {
@@ -629,13 +781,29 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
         cudaMemcpyAsync(v->front, front.data(), sizeof(uint32_t) * front.size(), cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(v->prefix, prefix.data(), sizeof(unsigned long long) * prefix.size(), cudaMemcpyHostToDevice,
                         s);
+        cudaMemcpyAsync(v->pprefix, pprefix.data(), sizeof(unsigned long long) * pprefix.size(),
+                        cudaMemcpyHostToDevice, s);
         if (!rel.empty())
             cudaMemcpyAsync(v->rel, rel.data(), sizeof(uint32_t) * rel.size(), cudaMemcpyHostToDevice, s);
         cudaMemcpyAsync(v->rel_off, rel_off.data(), sizeof(uint32_t) * rel_off.size(), cudaMemcpyHostToDevice, s);
         for (uint32_t k : act) cudaMemsetAsync(v->counts + k, 0, sizeof(uint32_t), s);
-        a.A = (uint32_t)act.size();
+        a.A = n_push;
         const unsigned long long items = prefix.back();
         if (items) k_serve_hop<<<grid_for((items + 31) / 32, kHopThreads / 32, 152u * 8u), kHopThreads, 0, s>>>(a);
+        const uint32_t n_pull = (uint32_t)act.size() - n_push;
+        if (n_pull) {
+            HopArgs b = a;
+            b.active = v->active + n_push;
+            b.rel_off = v->rel_off + n_push;
+            b.prefix = v->pprefix;
+            b.A = n_pull;
+            for (uint32_t i = n_push; i < act.size(); ++i) cudaMemsetAsync(v->ucount + act[i], 0, sizeof(unsigned), s);
+            const uint32_t nw = (N + 31) / 32;
+            k_serve_unvisited<<<dim3(std::min<uint32_t>((nw + 255) / 256, 1024u), n_pull), 256, 0, s>>>(b, v->ucount);
+            const unsigned long long objs = pprefix.back();
+            if (objs) k_serve_pull<<<grid_for(objs, 8, 152u * 16u), 256, 0, s>>>(b);
+            k_serve_mark<<<dim3(64, n_pull), 256, 0, s>>>(b);
+        }
         std::vector<uint32_t> cnt(v->slots);
         std::vector<unsigned long long> scanned(v->slots);
         cudaMemcpyAsync(cnt.data(), v->counts, sizeof(uint32_t) * v->slots, cudaMemcpyDeviceToHost, s);
@@ -674,6 +842,7 @@ extern "C" glint_status glint_server_step(glint_server *v, uint32_t *n_active, u
             st.hop_end[st.hop] = st.ids.size();
             ++st.hop;
             st.frontier = got;
+            st.reached += got;
             v->hparam[k].cur = nl;
             if (st.hop >= st.hops || got == 0) {
                 for (uint32_t h = st.hop; h < kMaxHops; ++h) st.hop_end[h] = st.ids.size();
@@ -741,6 +910,8 @@ void servers_detach(glint_ctx *c) {
         v->scanned = v->prefix = v->sprefix = nullptr;
         v->blocks = nullptr;
         v->rel = v->rel_off = v->front = nullptr;
+        v->pprefix = nullptr;
+        v->ucount = nullptr;
         v->ctx = nullptr;
     }
     c->servers.clear();

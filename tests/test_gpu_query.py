@@ -74,6 +74,23 @@ def test_query_matches_oracle_bfs():
     g.close()
 
 
+def test_pull_hops_equal_the_frontier_walk():
+    """Once a slot's frontier is at least as large as the set of objects it
+    has not reached, the hop runs from the unreached side: each of those
+    objects reads its own keys and stops at the first one whose target was
+    reached before the hop.  Whole-history and windowed queries whose seeds
+    cover most objects (a pull from the first hop), queries that switch at a
+    later hop, and every object as a seed all give the oracle's walk."""
+    g, n, windows = build_store("dense_20k", 50, (20, 35, 49))
+    edges = edges_of(np.concatenate(windows), g.map_box)
+    rng = np.random.default_rng(9)
+    queries = [(rng.choice(n, k, replace=False).astype(np.uint32), hops, t0, t1) for k, hops, t0, t1 in
+               [(15000, 2, 0, 0), (12000, 3, 10, 30), (10000, 2, 40, 49), (3000, 4, 0, 0), (800, 3, 0, 25),
+                (n, 1, 0, 0)]]
+    check(g, n, edges, queries)
+    g.close()
+
+
 def test_query_over_host_kept_blocks():
     """blocks beyond store_keep move to page-locked host memory (up to
     store_host_keep) and are still queried, read by the GPU over the host
