@@ -94,7 +94,7 @@ def test_parity_with_oracle(name):
 
 
 def test_parity_small_100k():
-    """BASELINE configs[0] (100k objects, 100 steps) against the oracle."""
+    """The small plain case (100k objects, 100 steps) against the oracle."""
     run_parity("small_100k", state_every=50)
 
 
@@ -167,12 +167,11 @@ def test_device_generator_matches_host():
     ob = g2.objects_bytes()
     h = ctypes.c_void_p()
     assert lib.glint_gen_create(pb, len(pb), ob, n, len(ob) // n, 0, ctypes.byref(h)) == 0
-    cudart = ctypes.CDLL("libcudart.so") if False else None  # noqa: F841
     import glint_pipeline_gb300 as gp
     bench_cfg = gp.Configuration(num_objects=n)
     b = gp.DeviceBench(bench_cfg, host.box(), ref[0])  # owns a stream and device memory we can borrow
     out = np.zeros((n, 2))
-    # generate into the bench's own input buffer through step_device: compare via a host copy
+    # generate each step on the bench's stream into a device buffer and compare a host copy
     for t in range(25):
         dptr = _device_buffer(n)
         assert lib.glint_gen_step(h, ctypes.c_void_p(dptr.ptr), ctypes.c_void_p(b.stream)) == 0

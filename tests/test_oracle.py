@@ -56,7 +56,7 @@ def test_oracle_matches_golden(name):
 
 
 def test_oracle_matches_golden_small_100k():
-    """BASELINE configs[0]: 100k objects x 100 steps, per-step digests."""
+    """The small plain case: 100k objects x 100 steps, per-step digests."""
     g = golden("small_100k")
     box, pts = make_points("small_100k")
     o = Oracle(make_config(**case_config("small_100k")), box, pts[0])

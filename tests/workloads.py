@@ -9,7 +9,7 @@ from glint_pipeline_gb300.tracegen import SEED_SMALL, TraceGenerator
 
 # name -> (seed, objects, steps, generator kind, box extent m, bucket count (0 = 2N), extra config)
 CASES = {
-    # BASELINE configs[0]: 100k objects, 100 steps, reach 2 m, min 5, B = 2N
+    # the small plain case: 100k objects, 100 steps, reach 2 m, min 5, B = 2N
     "small_100k": (SEED_SMALL, 100_000, 100, 0, None, 0, {}),
     # dense 4x4 km box: many splits/merges and cross-leaf checks
     "dense_20k": (0x1234, 20_000, 60, 0, 4000.0, 0, {}),
