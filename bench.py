@@ -913,17 +913,22 @@ def run_batch(args, local, K=None, W=None):
             continue
         rep = regions[members[len(members) // 2]]
 
+        # a trial steps through the trajectories generated above: `total`
+        # steps, half of them (at most three) untimed
+        tr_steps = min(6, total)
+        tr_warm = tr_steps // 2
+
         def trial(cfg, rep=rep):
             b = gp.DeviceBench(cfg, rep["box"], rep["first"])
-            for t in range(3):
+            for t in range(tr_warm):
                 b.step_device(rep["steps"].value + 16 * rep["n"] * t, t)
                 b.sync()
             rt.cudaDeviceSynchronize()
             t0 = time.perf_counter()
-            for t in range(3, 6):
+            for t in range(tr_warm, tr_steps):
                 b.step_device(rep["steps"].value + 16 * rep["n"] * t, t)
                 b.sync()
-            dt = (time.perf_counter() - t0) / 3
+            dt = (time.perf_counter() - t0) / (tr_steps - tr_warm)
             b.close()
             return dt
         best, table = autotune(lambda cap, lf, ch, n=rep["n"]: config(n, cap, lf, ch), trial,

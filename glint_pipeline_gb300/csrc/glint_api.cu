@@ -662,6 +662,22 @@ void begin_step(glint_ctx *c, uint32_t cur_time) {
     c->stats_valid = false;
 }
 
+/* the step's input must be device (or managed) memory: an address that is
+ * neither would reach the copy engine unchecked */
+bool device_points(glint_ctx *c, const void *p) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        c->last_error = "step input: not a CUDA pointer";
+        return false;
+    }
+    if (at.type != cudaMemoryTypeDevice && at.type != cudaMemoryTypeManaged) {
+        c->last_error = "step input: not device memory";
+        return false;
+    }
+    return true;
+}
+
 } // namespace glint
 
 extern "C" {
@@ -780,6 +796,7 @@ glint_status glint_step_device(glint_ctx *c, const double *d_points, uint32_t cu
     if (!c || !d_points) return GLINT_ERR_INVALID_ARGUMENT;
     if (serve_only_refused(c, "step")) return GLINT_ERR_STATE;
     cudaSetDevice(c->device);
+    if (!device_points(c, d_points)) return GLINT_ERR_INVALID_ARGUMENT;
     return enqueue_step(c, d_points, false, cur_time);
 }
 

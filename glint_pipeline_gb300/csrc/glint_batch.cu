@@ -173,11 +173,12 @@ extern "C" glint_ctx *glint_batch_region(glint_batch *b, uint32_t r) {
 extern "C" glint_status glint_batch_step(glint_batch *b, const double *const *d_points, uint32_t cur_time) {
     if (!b || !d_points) return GLINT_ERR_INVALID_ARGUMENT;
     const size_t R = b->regions.size();
+    cudaSetDevice(b->device);
     for (size_t r = 0; r < R; ++r) {
         if (!d_points[r]) return GLINT_ERR_INVALID_ARGUMENT;
         if (glint::serve_only_refused(b->regions[r], "batch step")) return GLINT_ERR_STATE;
+        if (!glint::device_points(b->regions[r], d_points[r])) return GLINT_ERR_INVALID_ARGUMENT;
     }
-    cudaSetDevice(b->device);
     /* the graph reads every region's step parameters from host memory when
      * it runs: the previous timestep must be done before they change */
     if (b->launched) {

@@ -302,6 +302,7 @@ cudaError_t launch_refine_precision_batch(const RefineArgs *d_args, uint32_t R, 
 void launch_step_front(glint_ctx *c, const double *points, bool host);
 void launch_step_back(glint_ctx *c);
 void begin_step(glint_ctx *c, uint32_t cur_time);
+bool device_points(glint_ctx *c, const void *p);
 cudaError_t launch_insert(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_identify(glint_ctx *c, uint32_t cur_time);
 cudaError_t launch_schema_update(glint_ctx *c, cudaStream_t s, void *scan_tmp);

@@ -11,7 +11,7 @@ import os
 import numpy as np
 import pytest
 
-from glint_pipeline_gb300 import Configuration, DeviceBench
+from glint_pipeline_gb300 import Configuration, DeviceBench, GlintError
 from oracle.bindings import Oracle, cantor_inverse, make_config
 from workloads import CASES, case_config, digest, make_points
 
@@ -152,6 +152,25 @@ def test_gpu_matches_reference_fixtures(name):
         assert (st.checks, st.meetings, st.num_taken_buckets, st.num_active_meetings, st.leaves, st.nodes) == \
             tuple(int(v) for v in gold["counts"][t])
     g.close()
+
+
+def test_step_device_refuses_host_memory():
+    """glint_step_device reads device memory only: a host array is refused
+    before anything is enqueued, and the context steps on afterwards as the
+    oracle does."""
+    box, pts = make_points("dense_20k", 3)
+    cfgd = case_config("dense_20k")
+    o = Oracle(make_config(**cfgd), box, pts[0])
+    g = DeviceBench(gpu_config(cfgd), box, pts[0])
+    host = np.ascontiguousarray(pts[0])
+    with pytest.raises(GlintError):
+        g.step_device(host.ctypes.data, 0)
+    for t in range(3):
+        o.step(pts[t], t)
+        g.step(pts[t], t)
+        compare_meetings(o.meetings(), g.meetings(), t)
+    g.close()
+    o.close()
 
 
 def test_device_generator_matches_host():
