@@ -202,7 +202,9 @@ const char *glint_last_error(const glint_ctx *ctx);
  * completes, with stats (may be NULL). */
 glint_status glint_step(glint_ctx *ctx, const double *points, uint32_t cur_time, glint_step_stats *stats);
 /* the same with points already in device memory; enqueues the step on the
- * context's stream and returns without waiting */
+ * context's stream and returns without waiting.  d_points must be device (or
+ * managed) memory, else GLINT_ERR_INVALID_ARGUMENT before anything is
+ * enqueued */
 glint_status glint_step_device(glint_ctx *ctx, const double *d_points, uint32_t cur_time);
 /* waits for enqueued steps; stats of the last one (may be NULL) */
 glint_status glint_sync(glint_ctx *ctx, glint_step_stats *stats);
@@ -574,7 +576,8 @@ glint_status glint_precision_probe(glint_ctx *ctx, uint32_t stride, glint_precis
 /* ---- batching form: many independent regions on one GPU ------------------
  * Each region is a context created from cfgs[r] (per-stage timing off; all on
  * the same device) with its own stream.  glint_batch_step enqueues one
- * timestep of every region for cur_time, reading d_points[r] (device memory),
+ * timestep of every region for cur_time, reading d_points[r] (device memory,
+ * else GLINT_ERR_INVALID_ARGUMENT before anything is enqueued),
  * as one CUDA graph captured at the first step: every region's stages up to
  * the refine stage, one refine launch over the work items of all regions in
  * precision_mode 1 (regions in mode 0 refine on their own streams), then
