@@ -136,11 +136,6 @@ struct SchemaBuilder {
     }
 };
 
-glint_status fail(glint_ctx *c, glint_status st, const char *msg) {
-    if (c) c->last_error = msg;
-    return st;
-}
-
 glint_status cuda_fail(glint_ctx *c, cudaError_t e, const char *where) {
     if (c) {
         c->last_error = std::string(where) + ": " + cudaGetErrorString(e);

@@ -55,15 +55,16 @@ struct HopArgs {
     uint32_t A;
 };
 
-/* marks target reached for slot s and appends it to the slot's next list
- * when it is new; the lanes that call together and append to the same slot
- * take their places with one atomic (a slot's counter is one address that
- * every new object of a large frontier would otherwise hit) */
+/* the reached-set word of target for slot s (all ones past N) */
 __device__ inline uint32_t visited_word(const HopArgs &a, uint32_t s, uint32_t target) {
     return target < a.N ? __ldcg(&a.visited[(size_t)s * a.words + (target >> 5)]) : ~0u;
 }
 
-/* as visit, with the target's bitmap word already read (visited_word) */
+/* marks target reached for slot s and appends it to the slot's next list
+ * when it is new, given its reached-set word `seen` (visited_word); the
+ * lanes that call together and append to the same slot take their places
+ * with one atomic (a slot's counter is one address that every new object of
+ * a large frontier would otherwise hit) */
 __device__ inline void visit_seen(const HopArgs &a, uint32_t s, uint32_t next_list, uint32_t target, uint32_t seen) {
     const unsigned calling = __activemask();
     bool fresh = false;
@@ -82,10 +83,6 @@ __device__ inline void visit_seen(const HopArgs &a, uint32_t s, uint32_t next_li
     base = __shfl_sync(peers, base, leader);
     const uint32_t idx = base + __popc(peers & ((1u << lane) - 1u));
     if (idx < a.N) a.lists[((size_t)s * 2 + next_list) * a.N + idx] = target;
-}
-
-__device__ inline void visit(const HopArgs &a, uint32_t s, uint32_t next_list, uint32_t target) {
-    visit_seen(a, s, next_list, target, visited_word(a, s, target));
 }
 
 /* one item's keys as the hop reads them: where they start, how many, and
