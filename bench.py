@@ -393,6 +393,12 @@ def roofline(form, N, buckets=None, mode=None):
             "traffic_unit": "DRAM bytes per step of the stage's kernels", "algorithmic_bytes": by,
             "model": "40 B/object + 32 B/contact pair + 48 B/meeting; the stage's share",
             "step_bytes": step_by, "frac_step": step_by / (form["ms_per_step"] / 1000.0) / 1e9 / peak,
+            # the model's flush term: 2 x 16 B per key and radix pass over the
+            # flushed keys (two per reported meeting), 16 passes of 8 bits for
+            # 128-bit keys, amortised over the steps
+            "flush_bytes_per_step": 2 * 16 * 16 * 2 * form["per_step"]["meetings"],
+            "frac_step_with_flush": (step_by + 2 * 16 * 16 * 2 * form["per_step"]["meetings"]) /
+                                    (form["ms_per_step"] / 1000.0) / 1e9 / peak,
             "traffic_over_algorithmic": ratio,
             "stage_model_bytes": stage_model,
             "stage_model": "bytes each stage's kernels must move in this design (table records, lists, "
