@@ -544,7 +544,9 @@ def workload_config(args, N, form):
                         f"min meeting 5, leaf capacity 50, {args.buckets} buckets, flush past 2^26 keys; "
                         f"headline form '{form}'",
             "objects": N, "buckets": args.buckets, "form": form,
-            "l2": "inputs larger than L2 (160 MB of points per step, 34 GB table)"}
+            "l2": (f"inputs larger than L2 ({16 * N / 1e6:.0f} MB of points per step, "
+                   f"{32 * args.buckets / 1e9:.1f} GB table)" if 32 * args.buckets > 129e6 else
+                   f"the table ({32 * args.buckets / 1e6:.0f} MB) fits in L2")}
 
 
 def poisson_stream(srv, rng, N, t_hi, rate, seconds, deadline_s):
