@@ -332,9 +332,11 @@ cudaError_t launch_insert(glint_ctx *c, uint32_t cur_time) {
     (void)cur_time;
     /* many short blocks: a thread's walk can be long (probe runs,
      * displacements), and with one resident wave of long grid-stride loops
-     * the slowest threads set the kernel's end; 152 x 128 blocks balance it
-     * (5.4 against 7.7 ms at 10M objects) */
-    k_insert<<<152 * 128, 256, 0, c->stream>>>(c->d_new, c->d_tab, c->d_newline, c->B, c->Bm, c->new_cap, c->d_fpos, c->N,
+     * the slowest threads set the kernel's end; up to 152 x 128 blocks
+     * balance it (5.4 against 7.7 ms at 10M objects), fewer for a small
+     * context's new-pair capacity */
+    const unsigned blocks = (unsigned)std::min<uint64_t>(152u * 128u, std::max<uint64_t>(152u, c->new_cap / 2048));
+    k_insert<<<blocks, 256, 0, c->stream>>>(c->d_new, c->d_tab, c->d_newline, c->B, c->Bm, c->new_cap, c->d_fpos, c->N,
                                              c->d_cnt);
     return cudaGetLastError();
 }
