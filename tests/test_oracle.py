@@ -179,3 +179,25 @@ def test_threaded_oracle_equals_single_thread(name, threads):
         assert reruns > 0
     one.close()
     many.close()
+
+
+@pytest.mark.skipif(not ref_available(), reason="the reference's sources are not on this machine")
+def test_calibration_script(tmp_path):
+    """oracle/calibrate_cpu.py times the reference's own CPU stages (-O2 and
+    as shipped) and the oracle on one host; on one thread all three report
+    the same meetings."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = tmp_path / "calibration.md"
+    r = subprocess.run([sys.executable, os.path.join(root, "oracle", "calibrate_cpu.py"), "--objects", "20000",
+                        "--buckets", "65536", "--steps", "2", "--warmup", "6", "--out", str(out)],
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    rows = [json.loads(line) for line in r.stdout.splitlines() if line.startswith("{")]
+    one = {row["label"]: row["meetings"] for row in rows if row["threads"] == 1}
+    assert set(one) == {"reference -O2", "reference as shipped (-g)", "port (oracle, -O2)"}
+    assert len(set(one.values())) == 1 and next(iter(one.values())) > 0
+    text = out.read_text()
+    assert "| reference -O2 | 1 |" in text and "| port (oracle, -O2) | 1 |" in text
