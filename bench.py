@@ -402,7 +402,7 @@ def roofline(form, N, buckets=None, mode=None):
             "traffic_over_algorithmic": ratio,
             "stage_model_bytes": stage_model,
             "stage_model": "bytes each stage's kernels must move in this design (table records, lists, "
-                           "stamps); the reference's model counts only the survey's per-unit figures",
+                           "stamps); the `model` above counts only 40 B/object, 32 B/contact and 48 B/meeting",
             "peak_source": "of measured (MEASURED_PEAKS.json hbm_gbs)" if hbm else "of fallback"}
 
 
